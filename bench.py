@@ -1,0 +1,319 @@
+#!/usr/bin/env python3
+"""Encrypted predictions/s of the party-B scoring step (cloud_compute_score,
+eval/idash.cpp:763-848) on GB300.
+
+One step = one pass of the scoring step over one batch: every output
+ciphertext of the model computed once.  Default workload (full scale, the
+reference's TRLWE-packed layout): 1,000 individuals packed in one region per
+TRLWE (N = 1024), 16,184 tag SNPs (48,552 input TRLWE), 80,882 targets x 3
+outputs (242,646 output TRLWE), 5 nearest-tag neighbours, coefficients
+uniform in [-8192, 8191]; synthetic seeded data.
+
+  value   predictions/s with inputs and model resident in HBM (CUDA events
+          on the launching stream; inputs 0.4 GB > L2, outputs 2 GB)
+  e2e     the same through idash_score_trlwe_host with page-locked host
+          buffers: every step copies the inputs in and the outputs out
+  roofline the scoring kernel against the measured HBM copy bandwidth
+  cpu_baseline the oracle's restatement of the reference loop on the host cores
+
+--impl reference times that CPU restatement alone (all host threads) on the
+same workload and prints the same line with impl=reference.
+Multi-GPU (torchrun): each rank scores its own batch of the same size
+(weak scaling, no collective on the data path); max time over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+WORKLOADS = {
+    "trlwe_full": dict(n_indiv=1000, n_tags=16184, n_targets=80882, neighbours=5,
+                       desc="full scale, TRLWE-packed (reference layout): 1,000 individuals, 16,184 tags, "
+                            "80,882 targets x 3 outputs, 5 neighbours, N=1024, NUM_REGIONS=1"),
+    "trlwe_r10": dict(n_indiv=100, n_tags=500, n_targets=2000, neighbours=5,
+                      desc="CPU-runnable size, TRLWE-packed: 100 individuals (NUM_REGIONS=10, REGION_SIZE=102), "
+                           "500 tags, 2,000 targets x 3 outputs, 5 neighbours"),
+}
+METRIC = "encrypted predictions/s (indiv x target x 3)"
+UNIT = "predictions/s"
+
+
+def peaks():
+    try:
+        p = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profiled_traffic(name: str):
+    """dram bytes per launch recorded from an ncu capture in profiles/<name>."""
+    path = os.path.join(ROOT, "profiles", name)
+    try:
+        for line in open(path):
+            if line.startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":", 1)[1].split()[0])
+    except OSError:
+        pass
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons, sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.samples = []
+        self.proc = None
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", str(device)], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9:
+                self.samples.append((time.time(), parts))
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self, t0: float, t1: float):
+        sel = [s for t, s in self.samples if t0 - 0.25 <= t <= t1 + 0.25]
+        if not sel and self.samples:
+            mid = (t0 + t1) / 2
+            sel = [min(self.samples, key=lambda ts: abs(ts[0] - mid))[1]]
+        if not sel:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        mhz = sorted(float(s[1]) for s in sel if s[1].replace(".", "").isdigit())
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in sel for i in range(4) if s[5 + i].lower().startswith("active")})
+        return {"sm_mhz": mhz[len(mhz) // 2] if mhz else None,
+                "sm_max_mhz": float(sel[0][2]) if sel[0][2].replace(".", "").isdigit() else None,
+                "reasons": reasons, "samples": len(sel)}
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", str(rank)))
+    return rank, world, local
+
+
+def cpu_baseline(model_csr, rows, spec, min_seconds=8.0, max_reps=20):
+    """The oracle's restatement of the reference loop (OpenMP over outputs,
+    eval/idash.cpp:779-842) on all host cores, full workload per rep."""
+    import pyoracle
+    cores = os.cpu_count() or 1
+    preds = spec["n_indiv"] * spec["n_targets"] * 3
+    reps, t0 = 0, time.perf_counter()
+    while True:
+        pyoracle.trlwe_score(model_csr.term_ptr, model_csr.term_feat, model_csr.term_coef, rows, spec["num_samples"],
+                             spec["regions"], spec["region_size"], n_threads=cores)
+        reps += 1
+        el = time.perf_counter() - t0
+        if el >= min_seconds or reps >= max_reps:
+            break
+    return {"value": preds * reps / el, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"{reps} full passes of the workload ({el:.1f} s), oracle/oracle.c restatement of "
+                      f"eval/idash.cpp:779-842, OpenMP {cores} threads"}
+
+
+def workload_spec(name):
+    spec = dict(WORKLOADS[name])
+    regions = max(1, 1024 // spec["n_indiv"])
+    spec.update(regions=regions, region_size=1024 // regions, num_samples=spec["n_indiv"],
+                n_rows=(3 * spec["n_tags"] + regions - 1) // regions)
+    return spec
+
+
+def run_reference(args):
+    import numpy as np
+    from idash2019_2_gb300 import gpu
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    spec = workload_spec(args.workload)
+    w = gpu.synth_model(args.seed, spec["n_tags"], spec["n_targets"], neighbours=spec["neighbours"])
+    rng = np.random.default_rng(args.seed)
+    rows = rng.integers(0, 2 ** 32, size=(spec["n_rows"], 2048), dtype=np.uint64).astype(np.uint32).view(np.int32)
+    import pyoracle
+    preds = spec["n_indiv"] * spec["n_targets"] * 3
+    cores = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        pyoracle.trlwe_score(w.model.term_ptr, w.model.term_feat, w.model.term_coef, rows, spec["num_samples"],
+                             spec["regions"], spec["region_size"], n_threads=cores)
+    steps = args.steps if args.steps_given else 3
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        pyoracle.trlwe_score(w.model.term_ptr, w.model.term_feat, w.model.term_coef, rows, spec["num_samples"],
+                             spec["regions"], spec["region_size"], n_threads=cores)
+    el = time.perf_counter() - t0
+    value = preds * steps / el
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": steps, "warmup": args.warmup,
+            "ms_per_step": el / steps * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "int32 (Z/2^32)", "data": "synthetic (seeded)", "impl": "reference",
+            "config": {"workload": spec["desc"]},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": f"{steps} full passes; oracle/oracle.c restatement of eval/idash.cpp:779-842 "
+                                       f"(the reference's TFHE dependency is absent, so its cloud binary cannot be "
+                                       f"built on this host)"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+    from idash2019_2_gb300 import gpu
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    torch.cuda.init()
+    spec = workload_spec(args.workload)
+    ctx = gpu.Context(local)
+    w = gpu.synth_model(args.seed + rank, spec["n_tags"], spec["n_targets"], neighbours=spec["neighbours"])
+    params = gpu.TrlweParams(1024, 1, spec["num_samples"], spec["regions"], spec["region_size"], 1 << 18, 42)
+    model = gpu.TrlweModel(ctx, w.model, spec["n_rows"], spec["num_samples"], spec["regions"], spec["region_size"])
+    d_in = ctx.device_alloc(spec["n_rows"] * 8192)
+    d_out = ctx.device_alloc(model.n_out * 8192)
+    gpu.synth_trlwe_device(ctx, args.seed + rank, params, spec["n_tags"], d_in.ptr, gpu.DENSE_TRLWE)
+    ctx.sync()
+    lay = gpu.DENSE_TRLWE
+    for _ in range(max(args.warmup, 3)):
+        model.score_device(d_in.ptr, lay, d_out.ptr, lay)
+    ctx.sync()
+    info = model.info()
+
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    sampler = ClockSampler(local)
+    time.sleep(0.3)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    ctx.sync()
+    launches0 = ctx.stats()["kernel_launches"]
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t0 = time.time()
+    e0.record(stream)
+    for _ in range(args.steps):
+        model.score_device(d_in.ptr, lay, d_out.ptr, lay)
+    e1.record(stream)
+    e1.synchronize()
+    t1 = time.time()
+    ctx.sync()
+    torch.cuda.synchronize()
+    launches = ctx.stats()["kernel_launches"] - launches0
+    ms = e0.elapsed_time(e1)
+    if world > 1:
+        tt = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        ms = float(tt.item())
+    time.sleep(0.25)
+    clocks = sampler.summary(t0, t1)
+    sampler.stop()
+    preds_per_step = spec["n_indiv"] * spec["n_targets"] * 3
+    ms_step = ms / args.steps
+    value = preds_per_step * world / (ms_step / 1e3)
+
+    # algorithmic bytes of one launch: each distinct input TRLWE read once,
+    # each output TRLWE written once, the model's CSR (4 B feature + 4 B
+    # coefficient per term, 4 B bias + 4 B row pointer per output)
+    alg_bytes = info["algorithmic_in_rows"] * 8192 + model.n_out * 8192 + info["n_terms"] * 8 + model.n_out * 8
+    peak, peak_src = peaks()
+    achieved = alg_bytes / (ms_step / 1e3) / 1e9
+    traffic = profiled_traffic("trlwe_window_full.txt")
+
+    # end to end through the host-memory entry point
+    e2e_steps = max(3, min(args.steps, 20))
+    h_in = ctx.host_alloc(spec["n_rows"] * 8192)
+    h_out = ctx.host_alloc(model.n_out * 8192)
+    h_in.array[:] = d_in.download()
+    model.score_host(h_in.ptr, lay, spec["n_rows"], h_out.ptr, lay)
+    st0 = ctx.stats()
+    if world > 1:
+        torch.distributed.barrier()
+    te0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        model.score_host(h_in.ptr, lay, spec["n_rows"], h_out.ptr, lay)
+    te = time.perf_counter() - te0
+    if world > 1:
+        tt = torch.tensor([te], device="cuda")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        te = float(tt.item())
+    st1 = ctx.stats()
+    e2e = {"value": preds_per_step * world * e2e_steps / te, "unit": UNIT,
+           "h2d_bytes_per_step": (st1["h2d_bytes"] - st0["h2d_bytes"]) // e2e_steps,
+           "d2h_bytes_per_step": (st1["d2h_bytes"] - st0["d2h_bytes"]) // e2e_steps,
+           "ms_per_step": te / e2e_steps * 1e3}
+
+    base = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        rows = np.frombuffer(h_in.array, dtype=np.int32).reshape(spec["n_rows"], 2048)
+        base = cpu_baseline(w.model, rows, spec)
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "int32 (Z/2^32)", "data": "synthetic (seeded)",
+                "config": {"workload": spec["desc"], "individuals": spec["n_indiv"], "targets": spec["n_targets"],
+                           "tags": spec["n_tags"], "neighbours": spec["neighbours"], "outputs": model.n_out,
+                           "input_rows": spec["n_rows"], "l2": "inputs 0.40 GB and outputs 1.99 GB exceed the 129 MB L2",
+                           "kernel": "window (batched, persistent, CUDA graph)" if info["kernel"] == 0 else "direct",
+                           "slice_words": info["slice_words"], "parallelism": f"{world} independent batch(es)"},
+                "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                             "frac": achieved / peak, "traffic": traffic, "peak_source": peak_src,
+                             "algorithmic_bytes_per_launch": alg_bytes},
+                "cpu_baseline": base, "e2e": e2e, "gpu_launches": launches, "clocks": clocks}
+        print(json.dumps(line), flush=True)
+    model.free()
+    ctx.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=None)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="trlwe_full")
+    ap.add_argument("--seed", type=int, default=0x1DA52019)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.steps_given = args.steps is not None
+    if args.steps is None:
+        args.steps = 2000
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,92 @@
+// Internal state behind the C ABI (include/idash_gpu.h).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/idash_gpu.h"
+#include "plan.hpp"
+#include "score_kernels.cuh"
+
+struct idash_ctx {
+    int device = 0;
+    int sm_count = 0;
+    size_t smem_optin = 0;  // max dynamic shared memory per CTA
+    cudaStream_t stream = nullptr, h2d = nullptr, d2h = nullptr;
+    cudaEvent_t join_in = nullptr, join_out = nullptr;
+    uint32_t *d_err = nullptr;
+    uint32_t *d_counters = nullptr;  // per-launch tile counters
+    static constexpr uint32_t kCounters = 256;
+    uint32_t next_counter = 0;
+
+    // options
+    int64_t opt_kernel = 0;        // 0 window (batched), 1 direct (plain)
+    int64_t opt_slice_words = 0;   // 0 = autotune
+    int64_t opt_ctas_per_sm = 0;   // 0 = autotune / occupancy
+    int64_t opt_graph = 1;
+    int64_t opt_max_window_slots = 0;
+    int64_t opt_max_group_terms = 0;
+
+    idash_stats stats{};
+    std::string last_error;
+
+    // buffers for the host-memory path (grow only)
+    uint8_t *d_in_buf = nullptr, *d_out_buf = nullptr;
+    size_t d_in_cap = 0, d_out_cap = 0;
+    std::vector<cudaEvent_t> events;
+
+    idash_status fail(idash_status s, const std::string &msg) {
+        last_error = msg;
+        return s;
+    }
+    idash_status check_cuda(cudaError_t e, const char *what) {
+        if (e == cudaSuccess) return IDASH_OK;
+        last_error = std::string(what) + ": " + cudaGetErrorString(e);
+        return e == cudaErrorMemoryAllocation ? IDASH_ERR_OUT_OF_MEMORY : IDASH_ERR_CUDA;
+    }
+    uint32_t *counter() { return d_counters + (next_counter++ % kCounters); }
+    cudaEvent_t event(size_t i);
+};
+
+struct idash_model {
+    idash_ctx *ctx = nullptr;
+    idash::Form form = idash::Form::kTrlwe;
+    idash_trlwe_params tp{};
+    idash_lwe_params lp{};
+    uint64_t n_out = 0, n_in_rows = 0;
+    std::vector<uint64_t> term_ptr;
+    std::vector<uint32_t> term_feat;
+    std::vector<int32_t> term_coef;
+    std::vector<uint32_t> out_index;
+    std::vector<uint32_t> out_row;
+    std::vector<uint32_t> row_of_index;
+
+    idash::Plan plan;
+    idash::KernelKind kind = idash::KernelKind::kWindow;
+    uint32_t slice_words = 1024, group_size = 3;
+    uint32_t max_slots = 0, max_terms = 0, max_groups = 0;
+    uint32_t ctas = 0;
+    bool tuned = false;
+
+    idash::PlanBlock *d_blocks = nullptr;
+    idash::PlanSlot *d_slots = nullptr;
+    idash::PlanGroup *d_groups = nullptr;
+    idash::PlanTerm *d_terms = nullptr;
+    uint64_t *d_var_ptr = nullptr;
+    uint32_t *d_var_row = nullptr;
+    int32_t *d_var_coef = nullptr;
+    uint32_t *d_out_index = nullptr;
+    uint32_t *d_out_row = nullptr;
+
+    // cached CUDA graph of the last device-path call
+    cudaGraphExec_t graph = nullptr;
+    const void *g_in = nullptr;
+    void *g_out = nullptr;
+    idash_row_layout g_in_layout{}, g_out_layout{};
+
+    void free_device();
+    void drop_graph();
+};

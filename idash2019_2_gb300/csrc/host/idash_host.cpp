@@ -1,0 +1,366 @@
+// Host side of the cloud step (see idash_host.hpp).
+#include "idash_host.hpp"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+
+namespace idash_host {
+
+namespace {
+
+double now_s() {
+    using namespace std::chrono;
+    return duration<double>(steady_clock::now().time_since_epoch()).count();
+}
+
+bool read_exact(std::istream &in, void *dst, size_t n) {
+    in.read(static_cast<char *>(dst), std::streamsize(n));
+    return size_t(in.gcount()) == n;
+}
+
+// "<pos>_<snp>" -> (pos, snp), as split() at eval/idash.cpp:50-57.
+bool split_feature(const std::string &s, uint64_t *pos, uint32_t *snp) {
+    const size_t k = s.find('_');
+    if (k == std::string::npos || k == 0 || k + 1 >= s.size()) return false;
+    char *end = nullptr;
+    const unsigned long long p = std::strtoull(s.c_str(), &end, 10);
+    if (end != s.c_str() + k) return false;
+    const unsigned long v = std::strtoul(s.c_str() + k + 1, &end, 10);
+    if (*end != '\0') return false;
+    *pos = p;
+    *snp = uint32_t(v);
+    return true;
+}
+
+// One .hr file into a name -> coefficient map, line by line as
+// eval/parse_vw.cpp:8-30 fills its map (later lines overwrite earlier ones).
+Status read_hr(const std::string &file, std::unordered_map<std::string, int32_t> *coefs) {
+    FILE *f = std::fopen(file.c_str(), "r");
+    if (!f) return Status::Err(IDASH_ERR_IO, "cannot open model file '" + file + "'");
+    char buf[256];
+    while (std::fgets(buf, sizeof(buf), f)) {
+        char name[256];
+        int value = 0;
+        if (std::sscanf(buf, "%255s %d", name, &value) != 2) continue;
+        (*coefs)[name] = int32_t(value);
+    }
+    std::fclose(f);
+    return Status::Ok();
+}
+
+}  // namespace
+
+RecordImage::~RecordImage() {
+    if (!data) return;
+    if (pinned) cudaFreeHost(data);
+    else std::free(data);
+}
+
+idash_status RecordImage::allocate(uint64_t n) {
+    const uint64_t need = 8 + n * kRecordBytes;
+    if (data && bytes >= need) {
+        count = n;
+        bytes = need;
+        return IDASH_OK;
+    }
+    if (data) {
+        if (pinned) cudaFreeHost(data);
+        else std::free(data);
+        data = nullptr;
+    }
+    void *p = nullptr;
+    if (cudaMallocHost(&p, need) == cudaSuccess) {
+        pinned = true;
+    } else {
+        cudaGetLastError();
+        pinned = false;
+        p = std::aligned_alloc(64, (need + 63) / 64 * 64);
+        if (!p) return IDASH_ERR_OUT_OF_MEMORY;
+    }
+    data = static_cast<uint8_t *>(p);
+    bytes = need;
+    count = n;
+    std::memcpy(data, &count, 8);
+    return IDASH_OK;
+}
+
+Status read_params(IdashParams &params, const std::string &filename) {
+    std::ifstream in(filename, std::ios::binary);
+    if (!in) return Status::Err(IDASH_ERR_IO, "cannot open parameters file '" + filename + "'");
+    uint32_t hdr[7];
+    if (!read_exact(in, hdr, sizeof(hdr))) return Status::Err(IDASH_ERR_FORMAT, "params.bin: truncated header");
+    params = IdashParams();
+    params.NUM_SAMPLES = hdr[0];
+    params.NUM_INPUT_POSITIONS = hdr[1];
+    params.NUM_OUTPUT_POSITIONS = hdr[2];
+    params.NUM_INPUT_FEATURES = hdr[3];
+    params.NUM_OUTPUT_FEATURES = hdr[4];
+    params.NUM_REGIONS = hdr[5];
+    params.REGION_SIZE = hdr[6];
+    for (uint32_t i = 0; i < params.NUM_INPUT_POSITIONS; ++i) {
+        uint64_t pos;
+        std::array<FeatBigIndex, 3> b;
+        if (!read_exact(in, &pos, 8) || !read_exact(in, b.data(), sizeof(b)))
+            return Status::Err(IDASH_ERR_FORMAT, "params.bin: truncated input table");
+        params.in_features_index.emplace(pos, std::array<FeatBigIndex, 3>());
+        params.in_features_index.at(pos) = b;
+    }
+    if (params.in_features_index.size() != params.NUM_INPUT_POSITIONS)
+        return Status::Err(IDASH_ERR_FORMAT, "params.bin: NUM_INPUT_POSITIONS != in_features_index.size()");
+    for (uint32_t i = 0; i < params.NUM_OUTPUT_POSITIONS; ++i) {
+        uint64_t pos;
+        if (!read_exact(in, &pos, 8)) return Status::Err(IDASH_ERR_FORMAT, "params.bin: truncated output table");
+        std::string name;
+        for (int c = in.get(); c > 0; c = in.get()) name.push_back(char(c));
+        std::array<FeatBigIndex, 3> b;
+        if (!read_exact(in, b.data(), sizeof(b)))
+            return Status::Err(IDASH_ERR_FORMAT, "params.bin: truncated output table");
+        params.out_position_names.push_back({pos, name});
+        params.out_features_index.emplace(pos, std::array<FeatBigIndex, 3>());
+        params.out_features_index.at(pos) = b;
+    }
+    if (params.out_features_index.size() != params.NUM_OUTPUT_POSITIONS ||
+        params.out_position_names.size() != params.NUM_OUTPUT_POSITIONS)
+        return Status::Err(IDASH_ERR_FORMAT, "params.bin: NUM_OUTPUT_POSITIONS != out_features_index.size()");
+    if (params.NUM_REGIONS == 0 || params.REGION_SIZE == 0 ||
+        uint64_t(params.NUM_REGIONS) * params.REGION_SIZE > IdashParams::N || params.NUM_SAMPLES > params.REGION_SIZE)
+        return Status::Err(IDASH_ERR_FORMAT, "params.bin: inconsistent NUM_REGIONS / REGION_SIZE / NUM_SAMPLES");
+    return Status::Ok();
+}
+
+Status write_params(const IdashParams &params, const std::string &filename) {
+    std::ofstream out(filename, std::ios::binary);
+    if (!out) return Status::Err(IDASH_ERR_IO, "cannot open parameters file '" + filename + "' for write");
+    const uint32_t hdr[7] = {params.NUM_SAMPLES,         params.NUM_INPUT_POSITIONS, params.NUM_OUTPUT_POSITIONS,
+                             params.NUM_INPUT_FEATURES,  params.NUM_OUTPUT_FEATURES, params.NUM_REGIONS,
+                             params.REGION_SIZE};
+    out.write(reinterpret_cast<const char *>(hdr), sizeof(hdr));
+    if (params.in_features_index.size() != params.NUM_INPUT_POSITIONS ||
+        params.out_features_index.size() != params.NUM_OUTPUT_POSITIONS ||
+        params.out_position_names.size() != params.NUM_OUTPUT_POSITIONS)
+        return Status::Err(IDASH_ERR_FORMAT, "params: position counts disagree with the index tables");
+    for (const auto &e : params.in_features_index) {
+        out.write(reinterpret_cast<const char *>(&e.first), 8);
+        out.write(reinterpret_cast<const char *>(e.second.data()), sizeof(e.second));
+    }
+    for (const auto &e : params.out_position_names) {
+        out.write(reinterpret_cast<const char *>(&e.first), 8);
+        out.write(e.second.c_str(), std::streamsize(e.second.size() + 1));
+        const auto &b = params.out_features_index.at(e.first);
+        out.write(reinterpret_cast<const char *>(b.data()), sizeof(b));
+    }
+    if (!out) return Status::Err(IDASH_ERR_IO, "write failed: '" + filename + "'");
+    return Status::Ok();
+}
+
+Status read_model(Model &model, const IdashParams &params, const std::string &path) {
+    for (const auto &elem : params.out_features_index) {
+        const uint64_t pos = elem.first;
+        for (uint32_t snp = 0; snp < 3; ++snp) {
+            std::unordered_map<std::string, int32_t> coefs;
+            Status st = read_hr(path + "/" + std::to_string(pos) + "_" + std::to_string(snp) + ".hr", &coefs);
+            if (!st.ok()) return st;
+            auto &mc = model.model[elem.second[snp]] = std::unordered_map<FeatBigIndex, int32_t>();
+            for (const auto &c : coefs) {
+                if (c.first == "Constant") {
+                    mc[IdashParams::constant_bigIndex()] = c.second;
+                    continue;
+                }
+                uint64_t in_pos;
+                uint32_t in_snp;
+                if (!split_feature(c.first, &in_pos, &in_snp))
+                    return Status::Err(IDASH_ERR_FORMAT, "model: bad feature name '" + c.first + "'");
+                const auto it = params.in_features_index.find(in_pos);
+                if (it == params.in_features_index.end() || in_snp >= 3)
+                    return Status::Err(IDASH_ERR_INDEX, "model: feature '" + c.first + "' is not a tag SNP of params");
+                mc[it->second[in_snp]] = c.second;
+            }
+        }
+    }
+    return Status::Ok();
+}
+
+static Status read_image(RecordImage &img, const std::string &filename) {
+    FILE *f = std::fopen(filename.c_str(), "rb");
+    if (!f) return Status::Err(IDASH_ERR_IO, "cannot open '" + filename + "'");
+    uint64_t count = 0;
+    if (std::fread(&count, 8, 1, f) != 1) {
+        std::fclose(f);
+        return Status::Err(IDASH_ERR_FORMAT, "'" + filename + "': missing record count");
+    }
+    std::fseek(f, 0, SEEK_END);
+    const long size = std::ftell(f);
+    std::fseek(f, 0, SEEK_SET);
+    if (size < 8 || uint64_t(size) != 8 + count * kRecordBytes) {
+        std::fclose(f);
+        return Status::Err(IDASH_ERR_FORMAT, "'" + filename + "': size is not 8 + count * 8208");
+    }
+    idash_status s = img.allocate(count);
+    if (s != IDASH_OK) {
+        std::fclose(f);
+        return Status::Err(s, "cannot allocate the record image");
+    }
+    const size_t got = std::fread(img.data, 1, size_t(size), f);
+    std::fclose(f);
+    if (got != size_t(size)) return Status::Err(IDASH_ERR_IO, "'" + filename + "': short read");
+    return Status::Ok();
+}
+
+Status read_encrypted_data(EncryptedData &data, const IdashParams &params, const std::string &filename) {
+    (void)params;
+    Status st = read_image(data.image, filename);
+    if (!st.ok()) return st;
+    data.record_of.clear();
+    data.record_of.reserve(data.image.count);
+    for (uint64_t i = 0; i < data.image.count; ++i) {
+        FeatIndex idx;
+        std::memcpy(&idx, data.image.record(i), 4);
+        data.record_of.emplace(idx, i);  // first record of an index wins, as eval/idash.cpp:531
+    }
+    return Status::Ok();
+}
+
+Status read_encrypted_predictions(EncryptedPredictions &preds, const std::string &filename) {
+    Status st = read_image(preds.image, filename);
+    if (!st.ok()) return st;
+    preds.record_of.clear();
+    for (uint64_t i = 0; i < preds.image.count; ++i) {
+        FeatBigIndex idx;
+        std::memcpy(&idx, preds.image.record(i), 4);
+        preds.record_of.emplace(idx, i);
+    }
+    return Status::Ok();
+}
+
+Status write_encrypted_predictions(const EncryptedPredictions &preds, const std::string &filename) {
+    FILE *f = std::fopen(filename.c_str(), "wb");
+    if (!f) return Status::Err(IDASH_ERR_IO, "cannot open '" + filename + "' for write");
+    const size_t put = preds.image.data ? std::fwrite(preds.image.data, 1, preds.image.bytes, f) : 0;
+    const bool ok = std::fclose(f) == 0 && put == preds.image.bytes;
+    if (!ok) return Status::Err(IDASH_ERR_IO, "short write to '" + filename + "'");
+    return Status::Ok();
+}
+
+Status cloud_compute_score(EncryptedPredictions &preds, const EncryptedData &data, const Model &model,
+                           const IdashParams &params, idash_ctx *ctx, CloudTiming *timing) {
+    if (!preds.record_of.empty()) return Status::Err(IDASH_ERR_STATE, "predictions must be empty on entry");
+    const double t0 = now_s();
+    // Record order of the output file: the reference creates one sample per
+    // model entry in model-iteration order (eval/idash.cpp:772-777) in an
+    // unordered_map and writes that map in its iteration order (:607).
+    std::unordered_map<FeatBigIndex, uint64_t> score;
+    for (const auto &it : model.model) score.emplace(it.first, 0);
+    uint64_t rec = 0;
+    for (auto &it : score) it.second = rec++;
+    const uint64_t n_out = score.size();
+
+    // Outputs numbered by FeatBigIndex (neighbouring targets adjacent); each
+    // output's terms in the model map's iteration order (the variance sum
+    // order of eval/idash.cpp:800-819).
+    std::vector<FeatBigIndex> outs;
+    outs.reserve(n_out);
+    for (const auto &it : model.model) outs.push_back(it.first);
+    std::sort(outs.begin(), outs.end());
+    std::vector<uint64_t> term_ptr(n_out + 1, 0);
+    std::vector<uint32_t> term_feat, out_row(n_out);
+    std::vector<int32_t> term_coef;
+    for (uint64_t o = 0; o < n_out; ++o) {
+        for (const auto &t : model.model.at(outs[o])) {
+            term_feat.push_back(t.first);
+            term_coef.push_back(t.second);
+        }
+        term_ptr[o + 1] = term_feat.size();
+        out_row[o] = uint32_t(score.at(outs[o]));
+    }
+    uint64_t n_index = 0;
+    for (const auto &it : data.record_of) n_index = std::max<uint64_t>(n_index, uint64_t(it.first) + 1);
+    std::vector<uint32_t> row_of_index(n_index, 0xFFFFFFFFu);
+    for (const auto &it : data.record_of) row_of_index[it.first] = uint32_t(it.second);
+
+    idash_trlwe_params tp{IdashParams::N, IdashParams::k, params.NUM_SAMPLES, params.NUM_REGIONS,
+                          params.REGION_SIZE, IdashParams::ONE_IN_T32, kTlweSampleTag};
+    idash_model *m = nullptr;
+    idash_status s = idash_model_trlwe(ctx, &m, &tp, n_out, outs.data(), out_row.data(), term_ptr.data(),
+                                       term_feat.data(), term_coef.data(), n_index, row_of_index.data(),
+                                       data.image.count);
+    if (s != IDASH_OK) return Status::Err(s, idash_last_error(ctx));
+    const double t1 = now_s();
+
+    s = preds.image.allocate(n_out);
+    void *d_in = nullptr, *d_out = nullptr;
+    if (s == IDASH_OK) s = idash_device_alloc(ctx, data.image.bytes, &d_in);
+    if (s == IDASH_OK) s = idash_device_alloc(ctx, preds.image.bytes, &d_out);
+    if (s == IDASH_OK) s = idash_copy_h2d(ctx, d_in, data.image.data, data.image.bytes);
+    idash_row_layout in_l = RecordImage::layout();
+    in_l.header_offset = -1;
+    const idash_row_layout out_l = RecordImage::layout();
+    if (s == IDASH_OK)
+        s = idash_score_trlwe_device(m, static_cast<uint8_t *>(d_in) + 8, &in_l, static_cast<uint8_t *>(d_out) + 8,
+                                     &out_l, nullptr);
+    if (s == IDASH_OK) s = idash_sync(ctx);
+    if (s == IDASH_OK) s = idash_copy_d2h(ctx, preds.image.data + 8, static_cast<uint8_t *>(d_out) + 8,
+                                          preds.image.bytes - 8);
+    Status st = s == IDASH_OK ? Status::Ok() : Status::Err(s, idash_last_error(ctx));
+    if (d_in) idash_device_free(ctx, d_in);
+    if (d_out) idash_device_free(ctx, d_out);
+    idash_model_free(m);
+    if (!st.ok()) return st;
+    std::memcpy(preds.image.data, &preds.image.count, 8);
+    preds.record_of.clear();
+    for (const auto &it : score) preds.record_of.emplace(it.first, it.second);
+    if (timing) {
+        timing->plan_s = t1 - t0;
+        timing->score_s = now_s() - t1;
+    }
+    return Status::Ok();
+}
+
+}  // namespace idash_host
+
+using namespace idash_host;
+
+extern "C" idash_status idash_cloud_files(int device, const char *params_file, const char *model_dir,
+                                          const char *data_file, const char *pred_file, idash_cloud_report *report,
+                                          char *errbuf, size_t errbuf_len) {
+    auto fail = [&](const Status &st) {
+        if (errbuf && errbuf_len) std::snprintf(errbuf, errbuf_len, "%s", st.message.c_str());
+        return st.code;
+    };
+    if (!params_file || !model_dir || !data_file || !pred_file)
+        return fail(Status::Err(IDASH_ERR_INVALID_ARGUMENT, "null file name"));
+    const double t0 = now_s();
+    idash_ctx *ctx = nullptr;
+    idash_status s = idash_open(&ctx, device);
+    if (s != IDASH_OK) return fail(Status::Err(s, idash_last_error(nullptr)));
+    IdashParams params;
+    Model model;
+    EncryptedData data;
+    EncryptedPredictions preds;
+    CloudTiming tm;
+    Status st = read_params(params, params_file);
+    if (st.ok()) st = read_model(model, params, model_dir);
+    if (st.ok()) st = read_encrypted_data(data, params, data_file);
+    const double t1 = now_s();
+    if (st.ok()) st = cloud_compute_score(preds, data, model, params, ctx, &tm);
+    const double t2 = now_s();
+    if (st.ok()) st = write_encrypted_predictions(preds, pred_file);
+    const double t3 = now_s();
+    idash_close(ctx);
+    if (!st.ok()) return fail(st);
+    if (report) {
+        report->read_s = t1 - t0;
+        report->plan_s = tm.plan_s;
+        report->score_s = tm.score_s;
+        report->write_s = t3 - t2;
+        report->n_in_records = data.image.count;
+        report->n_out_records = preds.image.count;
+    }
+    if (errbuf && errbuf_len) errbuf[0] = '\0';
+    return IDASH_OK;
+}

@@ -1,0 +1,105 @@
+// Host side of the cloud step, mirroring the reference's interface for it
+// (eval/idash.h): the same data roles, file formats and call sequence as
+// eval/cloud.cpp, with ciphertexts kept as contiguous record images so that
+// one copy moves them to or from the GPU.  Errors are returned, never
+// aborted on.
+#pragma once
+
+#include <array>
+#include <cstdint>
+#include <string>
+#include <unordered_map>
+#include <utility>
+#include <vector>
+
+#include "../../../include/idash_gpu.h"
+
+namespace idash_host {
+
+typedef uint32_t FeatBigIndex;  // eval/idash.h:40
+typedef uint32_t FeatIndex;     // eval/idash.h:41
+
+// Size of one ciphertext record in encrypted_data.bin and
+// encrypted_prediction.bin: uint32 index, int32 tag, 2N int32, double.
+constexpr uint64_t kRecordBytes = 8 + 2 * 1024 * 4 + 8;  // 8208
+constexpr int32_t kTlweSampleTag = 42;  // record tag of the ciphertext stream format
+
+// eval/idash.h:45-111 (the fields the cloud step reads).
+struct IdashParams {
+    static constexpr uint32_t N = 1024;
+    static constexpr uint32_t k = 1;
+    static constexpr int32_t ONE_IN_T32 = 1 << 18;  // dtot32(2^-14), eval/idash.cpp:39
+    uint32_t NUM_SAMPLES = 0, NUM_INPUT_POSITIONS = 0, NUM_OUTPUT_POSITIONS = 0;
+    uint32_t NUM_INPUT_FEATURES = 0, NUM_OUTPUT_FEATURES = 0, NUM_REGIONS = 0, REGION_SIZE = 0;
+    std::unordered_map<uint64_t, std::array<FeatBigIndex, 3>> in_features_index;
+    std::unordered_map<uint64_t, std::array<FeatBigIndex, 3>> out_features_index;
+    std::vector<std::pair<uint64_t, std::string>> out_position_names;
+
+    FeatIndex feature_indexOf(FeatBigIndex b) const { return b / NUM_REGIONS; }
+    uint32_t feature_regionOf(FeatBigIndex b) const { return b % NUM_REGIONS; }
+    static FeatBigIndex constant_bigIndex() { return 0xFFFFFFFFu; }
+};
+
+// eval/idash.h:129-134: per output, input feature -> integer coefficient.
+struct Model {
+    std::unordered_map<FeatBigIndex, std::unordered_map<FeatBigIndex, int32_t>> model;
+};
+
+// A ciphertext file held as one image: 8-byte count, then `count` records.
+struct RecordImage {
+    uint8_t *data = nullptr;  // 16-byte aligned (pinned when a GPU is present)
+    uint64_t bytes = 0, count = 0;
+    bool pinned = false;
+    RecordImage() = default;
+    RecordImage(const RecordImage &) = delete;
+    RecordImage &operator=(const RecordImage &) = delete;
+    ~RecordImage();
+    idash_status allocate(uint64_t count);
+    uint8_t *record(uint64_t i) const { return data + 8 + i * kRecordBytes; }
+    static idash_row_layout layout() { return idash_row_layout{kRecordBytes, 8, 8 + 2 * 1024 * 4, 0}; }
+};
+
+// eval/idash.h:136-167: FeatIndex -> the record that holds that TRLWE.
+struct EncryptedData {
+    RecordImage image;
+    std::unordered_map<FeatIndex, uint64_t> record_of;
+};
+
+// eval/idash.h:169-188: FeatBigIndex -> output record.
+struct EncryptedPredictions {
+    RecordImage image;
+    std::unordered_map<FeatBigIndex, uint64_t> record_of;
+};
+
+struct Status {
+    idash_status code = IDASH_OK;
+    std::string message;
+    bool ok() const { return code == IDASH_OK; }
+    static Status Ok() { return Status(); }
+    static Status Err(idash_status c, std::string m) { return Status{c, std::move(m)}; }
+};
+
+// params.bin (eval/idash.cpp:128-186, 200-261).
+Status read_params(IdashParams &params, const std::string &filename);
+Status write_params(const IdashParams &params, const std::string &filename);
+// <dir>/<pos>_<snp>.hr for every output position (eval/idash.cpp:66-114,
+// eval/parse_vw.cpp:8-30).
+Status read_model(Model &model, const IdashParams &params, const std::string &path);
+// encrypted_data.bin / encrypted_prediction.bin (eval/idash.cpp:513-613):
+// one bulk read / write of the whole image.
+Status read_encrypted_data(EncryptedData &data, const IdashParams &params, const std::string &filename);
+Status write_encrypted_predictions(const EncryptedPredictions &preds, const std::string &filename);
+Status read_encrypted_predictions(EncryptedPredictions &preds, const std::string &filename);
+
+struct CloudTiming {
+    double plan_s = 0, score_s = 0;  // model planning; copies + kernels
+};
+
+// eval/idash.h:251-252 / eval/idash.cpp:763-848 on the GPU behind the C ABI.
+// `preds` must be empty on entry.  Records come out in the order the
+// reference's EncryptedPredictions map iterates, so the written file matches
+// the reference's byte for byte.
+Status cloud_compute_score(EncryptedPredictions &preds, const EncryptedData &data, const Model &model,
+                           const IdashParams &params, idash_ctx *ctx, CloudTiming *timing = nullptr);
+
+}  // namespace idash_host

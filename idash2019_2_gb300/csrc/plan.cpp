@@ -1,0 +1,217 @@
+// Host planner (see plan.hpp).  Pure C++, no CUDA.
+#include "plan.hpp"
+
+#include <algorithm>
+#include <cstring>
+
+namespace idash {
+
+namespace {
+
+inline uint64_t make_key(uint32_t row, uint32_t rot) { return (uint64_t(row) << 32) | rot; }
+
+// Size of the union of two sorted key lists.
+size_t union_size(const uint64_t *a, size_t na, const uint64_t *b, size_t nb) {
+    size_t i = 0, j = 0, n = 0;
+    while (i < na && j < nb) {
+        if (a[i] < b[j]) ++i;
+        else if (b[j] < a[i]) ++j;
+        else { ++i; ++j; }
+        ++n;
+    }
+    return n + (na - i) + (nb - j);
+}
+
+}  // namespace
+
+std::string build_plan(const PlanInput &in, const PlanLimits &lim, Plan *plan, bool *index_error) {
+    *index_error = false;
+    *plan = Plan();
+    if (lim.group_size != 1 && lim.group_size != 3) return "group_size must be 1 or 3";
+    if (in.n_out >= kNoOutput) return "too many outputs";
+    if (in.form == Form::kTrlwe) {
+        if (in.num_regions == 0 || in.region_size == 0 ||
+            uint64_t(in.num_regions) * in.region_size > in.N)
+            return "NUM_REGIONS * REGION_SIZE must be in [1, N]";
+    }
+    const uint64_t n_out = in.n_out;
+    plan->n_terms_in = n_out ? in.term_ptr[n_out] - in.term_ptr[0] : 0;
+
+    // 1. Normalise every output: (slot key, coefficient) sorted by key,
+    //    duplicates summed mod 2^32, zero coefficients dropped, constants
+    //    folded into the bias.
+    std::vector<uint64_t> nptr(n_out + 1, 0);
+    std::vector<uint64_t> nkey;
+    std::vector<uint32_t> ncoef;
+    std::vector<uint32_t> bias(n_out, 0);
+    nkey.reserve(plan->n_terms_in);
+    ncoef.reserve(plan->n_terms_in);
+    std::vector<std::pair<uint64_t, uint32_t>> tmp;
+    if (in.form == Form::kTrlwe) plan->var_ptr.assign(n_out + 1, 0);
+    for (uint64_t o = 0; o < n_out; ++o) {
+        tmp.clear();
+        if (in.term_ptr[o + 1] < in.term_ptr[o]) return "term_ptr must be non-decreasing";
+        for (uint64_t t = in.term_ptr[o]; t < in.term_ptr[o + 1]; ++t) {
+            const uint32_t feat = in.term_feat[t];
+            const uint32_t coef = uint32_t(in.term_coef[t]);
+            if (feat == kConstantFeature) {
+                bias[o] += coef * uint32_t(in.one_t32);
+                continue;
+            }
+            uint64_t row;
+            uint32_t rot = 0;
+            if (in.form == Form::kTrlwe) {
+                const uint64_t index = feat / in.num_regions;
+                const uint32_t region = feat % in.num_regions;
+                if (in.row_of_index) {
+                    if (index >= in.n_index) { *index_error = true; return "feature index has no input ciphertext"; }
+                    row = in.row_of_index[index];
+                } else {
+                    row = index;
+                }
+                rot = region * in.region_size;
+                if (region == 0) {
+                    plan->var_row.push_back(uint32_t(row));
+                    plan->var_coef.push_back(in.term_coef[t]);
+                }
+            } else {
+                row = feat;
+            }
+            if (row >= in.n_rows || row >= 0xFFFFFFFFull) {
+                *index_error = true;
+                return "feature maps to an input row outside the input";
+            }
+            tmp.emplace_back(make_key(uint32_t(row), rot), coef);
+        }
+        if (in.form == Form::kTrlwe) plan->var_ptr[o + 1] = plan->var_row.size();
+        std::sort(tmp.begin(), tmp.end(),
+                  [](const std::pair<uint64_t, uint32_t> &x, const std::pair<uint64_t, uint32_t> &y) {
+                      return x.first < y.first;
+                  });
+        for (size_t i = 0; i < tmp.size();) {
+            size_t j = i;
+            uint32_t c = 0;
+            while (j < tmp.size() && tmp[j].first == tmp[i].first) c += tmp[j++].second;
+            if (c != 0) {
+                nkey.push_back(tmp[i].first);
+                ncoef.push_back(c);
+            }
+            i = j;
+        }
+        nptr[o + 1] = nkey.size();
+    }
+    {
+        std::vector<uint8_t> seen(in.n_rows, 0);
+        for (uint64_t k : nkey) seen[k >> 32] = 1;
+        uint64_t d = 0;
+        for (uint8_t s : seen) d += s;
+        plan->distinct_rows = d;
+    }
+
+    // 2. Groups of up to group_size consecutive outputs with (nearly) the
+    //    same slot set: union no larger than 5/4 of the largest member + 1.
+    struct G {
+        uint64_t o0;
+        uint32_t n;
+        std::vector<uint64_t> keys;
+        std::vector<uint32_t> c[3];
+    };
+    std::vector<G> groups;
+    groups.reserve(n_out / lim.group_size + 1);
+    for (uint64_t o = 0; o < n_out;) {
+        uint32_t n = 1;
+        std::vector<uint64_t> keys(nkey.begin() + nptr[o], nkey.begin() + nptr[o + 1]);
+        size_t largest = keys.size();
+        while (n < lim.group_size && o + n < n_out) {
+            const uint64_t p = o + n;
+            const size_t np = nptr[p + 1] - nptr[p];
+            const size_t u = union_size(keys.data(), keys.size(), nkey.data() + nptr[p], np);
+            const size_t big = std::max(largest, np);
+            if (u > big + big / 4 + 1 || u > lim.max_slots || u > lim.max_terms) break;
+            std::vector<uint64_t> merged;
+            merged.reserve(u);
+            std::set_union(keys.begin(), keys.end(), nkey.begin() + nptr[p], nkey.begin() + nptr[p + 1],
+                           std::back_inserter(merged));
+            keys.swap(merged);
+            largest = big;
+            ++n;
+        }
+        G g;
+        g.o0 = o;
+        g.n = n;
+        g.keys = keys;
+        for (uint32_t m = 0; m < 3; ++m) g.c[m].assign(keys.size(), 0);
+        for (uint32_t m = 0; m < n; ++m) {
+            const uint64_t p = o + m;
+            size_t idx = 0;
+            for (uint64_t t = nptr[p]; t < nptr[p + 1]; ++t) {
+                while (g.keys[idx] != nkey[t]) ++idx;
+                g.c[m][idx] = ncoef[t];
+            }
+        }
+        if (keys.size() > lim.max_slots || keys.size() > lim.max_terms)
+            return "an output needs more window slots than one block holds";
+        groups.push_back(std::move(g));
+        o += n;
+    }
+
+    // 3. Blocks of consecutive groups sharing one window of slots.
+    std::vector<uint64_t> win;
+    size_t gi = 0;
+    while (gi < groups.size()) {
+        PlanBlock b{};
+        b.group_begin = uint32_t(plan->groups.size());
+        b.term_begin = uint32_t(plan->terms.size());
+        b.slot_begin = uint32_t(plan->slots.size());
+        win.clear();
+        size_t gend = gi;
+        uint32_t terms = 0;
+        while (gend < groups.size()) {
+            const G &g = groups[gend];
+            const size_t u = union_size(win.data(), win.size(), g.keys.data(), g.keys.size());
+            if (gend > gi && (u > lim.max_slots || terms + g.keys.size() > lim.max_terms ||
+                              gend - gi + 1 > lim.max_groups))
+                break;
+            std::vector<uint64_t> merged;
+            merged.reserve(u);
+            std::set_union(win.begin(), win.end(), g.keys.begin(), g.keys.end(), std::back_inserter(merged));
+            win.swap(merged);
+            terms += uint32_t(g.keys.size());
+            ++gend;
+        }
+        b.n_slots = uint32_t(win.size());
+        uint32_t max_row = 0;
+        for (uint64_t k : win) {
+            plan->slots.push_back(PlanSlot{uint32_t(k >> 32), uint32_t(k & 0xFFFFFFFFu)});
+            max_row = std::max(max_row, uint32_t(k >> 32));
+        }
+        plan->block_max_row.push_back(max_row);
+        b.out_lo = uint32_t(groups[gi].o0);
+        b.out_hi = uint32_t(groups[gend - 1].o0 + groups[gend - 1].n);
+        for (size_t q = gi; q < gend; ++q) {
+            const G &g = groups[q];
+            PlanGroup pg{};
+            pg.term_begin = uint32_t(plan->terms.size()) - b.term_begin;
+            pg.n_terms = uint32_t(g.keys.size());
+            for (uint32_t m = 0; m < 3; ++m) {
+                pg.out[m] = m < g.n ? uint32_t(g.o0 + m) : kNoOutput;
+                pg.bias[m] = m < g.n ? int32_t(bias[g.o0 + m]) : 0;
+            }
+            for (size_t t = 0; t < g.keys.size(); ++t) {
+                const uint32_t local = uint32_t(std::lower_bound(win.begin(), win.end(), g.keys[t]) - win.begin());
+                plan->terms.push_back(PlanTerm{int32_t(g.c[0][t]), int32_t(g.c[1][t]), int32_t(g.c[2][t]), local});
+            }
+            plan->groups.push_back(pg);
+        }
+        b.n_groups = uint32_t(gend - gi);
+        b.n_terms = uint32_t(plan->terms.size()) - b.term_begin;
+        plan->max_block_slots = std::max(plan->max_block_slots, b.n_slots);
+        plan->max_block_terms = std::max(plan->max_block_terms, b.n_terms);
+        plan->max_block_groups = std::max(plan->max_block_groups, b.n_groups);
+        plan->blocks.push_back(b);
+        gi = gend;
+    }
+    return "";
+}
+
+}  // namespace idash

@@ -1,0 +1,374 @@
+// Scoring kernels: out_o = sum_terms coef * X^(-m) * row + bias, per column
+// slice of the ciphertext rows, all in Z/2^32.  This is the arithmetic of
+// cloud_compute_score (eval/idash.cpp:800-841) reorganised for the GPU:
+//   - tLweAddMulTo per term (eval/idash.cpp:817) becomes one IMAD per word;
+//   - the fold of region r (torusPolynomialMulByXai by 2N - r*REGION_SIZE then
+//     tLweAddTo, :826-836) is applied per term as a rotated read, which is the
+//     same value because the rotation is linear over Z/2^32;
+//   - the bias on b[0..NUM_SAMPLES) (:805-810) and the zeroing of
+//     b[REGION_SIZE..N) (:839-841) are the epilogue.
+//
+// k_score_window  (batched): persistent CTAs pull (block, slice) tiles from an
+//   atomic counter; each tile's input window is staged into shared memory with
+//   cp.async.bulk (completed on an mbarrier, waits bounded), then every thread
+//   accumulates 8 columns x G outputs with 16-byte shared-memory loads.
+// k_score_direct  (plain): one CTA per tile, each output read straight from
+//   global memory term by term - the reference's per-output loop on the GPU.
+#include "common.cuh"
+#include "score_kernels.cuh"
+
+namespace idash {
+
+namespace {
+
+constexpr int kThreads = 256;
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.expect_tx.relaxed.cta.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+
+// Epilogue masks for the 8 columns a thread owns (bits 0-3: q0..q0+3,
+// bits 4-7: q1..q1+3): which columns receive the bias, which are zeroed.
+__device__ __forceinline__ void column_masks(const ScoreArgs &a, uint32_t c0, uint32_t q0, uint32_t q1,
+                                             uint32_t &bias_mask, uint32_t &zero_mask) {
+    bias_mask = 0;
+    zero_mask = 0;
+#pragma unroll
+    for (int e = 0; e < 8; ++e) {
+        const uint32_t c = c0 + (e < 4 ? q0 + e : q1 + (e - 4));
+        if (a.form == kFormTrlwe) {
+            if (c >= a.N) {
+                const uint32_t j = c - a.N;
+                if (j < a.num_samples) bias_mask |= 1u << e;
+                if (j >= a.region_size) zero_mask |= 1u << e;
+            }
+        } else {
+            if (c % a.lwe_n1 == a.lwe_n1 - 1) bias_mask |= 1u << e;
+        }
+    }
+}
+
+__device__ __forceinline__ void store_quad(uint8_t *row, uint32_t q, uint32_t valid, uint4 v) {
+    if (q + 4 <= valid) {
+        stg_cs_v4(row + size_t(q) * 4, make_int4(int(v.x), int(v.y), int(v.z), int(v.w)));
+    } else {
+        uint32_t *p = reinterpret_cast<uint32_t *>(row) + q;
+        if (q + 0 < valid) p[0] = v.x;
+        if (q + 1 < valid) p[1] = v.y;
+        if (q + 2 < valid) p[2] = v.z;
+        if (q + 3 < valid) p[3] = v.w;
+    }
+}
+
+template <int G>
+__device__ __forceinline__ void write_outputs(const ScoreArgs &a, const PlanGroup &gr, const uint32_t (&acc)[G][8],
+                                              uint32_t c0, uint32_t q0, uint32_t q1, uint32_t valid,
+                                              uint32_t bias_mask, uint32_t zero_mask) {
+#pragma unroll
+    for (int m = 0; m < G; ++m) {
+        const uint32_t o = gr.out[m];
+        if (o == kNoOutput || o < a.out_lo || o >= a.out_hi) continue;
+        const uint32_t bias = uint32_t(gr.bias[m]);
+        uint32_t v[8];
+#pragma unroll
+        for (int e = 0; e < 8; ++e) {
+            uint32_t x = acc[m][e];
+            if (bias_mask & (1u << e)) x += bias;
+            if (zero_mask & (1u << e)) x = 0;
+            v[e] = x;
+        }
+        const uint64_t r = a.out_row_map ? uint64_t(a.out_row_map[o]) : uint64_t(o) - a.out_row_base;
+        uint8_t *row = a.out + r * a.out_stride + uint64_t(c0) * 4;
+        if (q0 < valid) store_quad(row, q0, valid, make_uint4(v[0], v[1], v[2], v[3]));
+        if (q1 < valid) store_quad(row, q1, valid, make_uint4(v[4], v[5], v[6], v[7]));
+    }
+}
+
+template <int G>
+__device__ __forceinline__ void mac8(uint32_t (&acc)[G][8], const PlanTerm &tm, const uint4 &x0, const uint4 &x1) {
+    const uint32_t c[3] = {uint32_t(tm.c0), uint32_t(tm.c1), uint32_t(tm.c2)};
+#pragma unroll
+    for (int m = 0; m < G; ++m) {
+        acc[m][0] += c[m] * x0.x;
+        acc[m][1] += c[m] * x0.y;
+        acc[m][2] += c[m] * x0.z;
+        acc[m][3] += c[m] * x0.w;
+        acc[m][4] += c[m] * x1.x;
+        acc[m][5] += c[m] * x1.y;
+        acc[m][6] += c[m] * x1.z;
+        acc[m][7] += c[m] * x1.w;
+    }
+}
+
+// Value of column c (of the 2N-word TRLWE row) of X^(-m) * row:
+// (X^(-m) P)[j] = P[j+m] if j+m < N else -P[j+m-N], per polynomial.
+__device__ __forceinline__ uint32_t rotated_word(const uint32_t *src, uint32_t c, uint32_t m, uint32_t N) {
+    const uint32_t p = c >= N ? 1u : 0u;
+    const uint32_t j = c - p * N;
+    const uint32_t t = j + m;
+    return t < N ? src[p * N + t] : 0u - src[p * N + t - N];
+}
+
+template <int W, int G>
+__global__ void __launch_bounds__(kThreads) k_score_window(const ScoreArgs a) {
+    constexpr int TEAM = W / 8;
+    constexpr int NTEAMS = kThreads / TEAM;
+    extern __shared__ __align__(128) uint8_t smem[];
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem);
+    uint32_t *tile_s = reinterpret_cast<uint32_t *>(smem + 8);
+    uint32_t *win = reinterpret_cast<uint32_t *>(smem + 128);
+    PlanTerm *terms_s = reinterpret_cast<PlanTerm *>(smem + 128 + size_t(a.max_slots) * W * 4);
+    PlanGroup *groups_s = reinterpret_cast<PlanGroup *>(terms_s + a.max_terms);
+
+    const uint32_t tid = threadIdx.x;
+    if (tid == 0) {
+        mbar_init(bar, 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+
+    const uint32_t team = tid / TEAM, lane = tid % TEAM;
+    const uint32_t q0 = 4 * lane, q1 = 4 * lane + 4 * TEAM;
+    uint32_t phase = 0;
+
+    for (;;) {
+        if (tid == 0) *tile_s = atomicAdd(a.tile_counter, 1u);
+        __syncthreads();
+        const uint32_t tile = *tile_s;
+        if (tile >= a.n_tiles) break;
+        const uint32_t b = a.block_lo + tile % a.n_blocks;
+        const uint32_t slice = tile / a.n_blocks;
+        const PlanBlock blk = a.blocks[b];
+        const uint32_t c0 = slice * W;
+        const uint32_t valid = min(uint32_t(W), a.row_words - c0);
+        const uint32_t copy_bytes = ((valid + 3u) & ~3u) * 4u;
+
+        // Producer warp: bulk-copy the block's terms, groups and the
+        // unrotated slots' column slices; lane 0 arrives once all lanes
+        // registered their transaction bytes.
+        if (tid < 32) {
+            if (tid == 0) fence_proxy_async_smem();
+            __syncwarp();
+            for (uint32_t s = tid; s < blk.n_slots; s += 32) {
+                const PlanSlot sl = a.slots[blk.slot_begin + s];
+                if (sl.rot != 0) continue;
+                if (sl.row >= a.n_rows) {
+                    report_error(a.err, kDevBadIndex);
+                    continue;
+                }
+                mbar_expect_tx(bar, copy_bytes);
+                bulk_g2s(win + size_t(s) * W, a.in + uint64_t(sl.row) * a.in_stride + uint64_t(c0) * 4, copy_bytes,
+                         bar);
+            }
+            if (tid == 0) {
+                if (blk.n_terms) {
+                    mbar_expect_tx(bar, blk.n_terms * uint32_t(sizeof(PlanTerm)));
+                    bulk_g2s(terms_s, a.terms + blk.term_begin, blk.n_terms * uint32_t(sizeof(PlanTerm)), bar);
+                }
+                mbar_expect_tx(bar, blk.n_groups * uint32_t(sizeof(PlanGroup)));
+                bulk_g2s(groups_s, a.groups + blk.group_begin, blk.n_groups * uint32_t(sizeof(PlanGroup)), bar);
+            }
+            __syncwarp();
+            if (tid == 0) mbar_arrive(bar);
+        }
+        // Rotated slots (TRLWE with NUM_REGIONS > 1): gathered by all threads.
+        if (a.form == kFormTrlwe) {
+            for (uint32_t s = 0; s < blk.n_slots; ++s) {
+                const PlanSlot sl = a.slots[blk.slot_begin + s];
+                if (sl.rot == 0 || sl.row >= a.n_rows) continue;
+                const uint32_t *src = reinterpret_cast<const uint32_t *>(a.in + uint64_t(sl.row) * a.in_stride);
+                for (uint32_t x = tid; x < valid; x += kThreads) win[size_t(s) * W + x] = rotated_word(src, c0 + x, sl.rot, a.N);
+            }
+        }
+        __syncthreads();
+        const bool ok = mbar_wait_bounded(bar, phase, a.err);
+        if (__syncthreads_or(!ok)) {
+            // A copy never completed: wait (bounded) once more so no copy is
+            // still writing shared memory when the CTA exits.
+            mbar_wait_bounded(bar, phase, nullptr);
+            return;
+        }
+        phase ^= 1u;
+
+        uint32_t bias_mask, zero_mask;
+        column_masks(a, c0, q0, q1, bias_mask, zero_mask);
+        for (uint32_t g = team; g < blk.n_groups; g += NTEAMS) {
+            const PlanGroup gr = groups_s[g];
+            uint32_t acc[G][8];
+#pragma unroll
+            for (int m = 0; m < G; ++m)
+#pragma unroll
+                for (int e = 0; e < 8; ++e) acc[m][e] = 0;
+            const PlanTerm *tp = terms_s + gr.term_begin;
+#pragma unroll 2
+            for (uint32_t t = 0; t < gr.n_terms; ++t) {
+                const PlanTerm tm = tp[t];
+                const uint32_t *w = win + size_t(tm.slot) * W;
+                const uint4 x0 = *reinterpret_cast<const uint4 *>(w + q0);
+                const uint4 x1 = *reinterpret_cast<const uint4 *>(w + q1);
+                mac8<G>(acc, tm, x0, x1);
+            }
+            write_outputs<G>(a, gr, acc, c0, q0, q1, valid, bias_mask, zero_mask);
+        }
+        __syncthreads();
+    }
+}
+
+template <int W, int G>
+__global__ void __launch_bounds__(kThreads) k_score_direct(const ScoreArgs a) {
+    constexpr int TEAM = W / 8;
+    constexpr int NTEAMS = kThreads / TEAM;
+    const uint32_t tid = threadIdx.x;
+    const uint32_t team = tid / TEAM, lane = tid % TEAM;
+    const uint32_t q0 = 4 * lane, q1 = 4 * lane + 4 * TEAM;
+    const uint32_t tile = blockIdx.x;
+    if (tile >= a.n_tiles) return;
+    const uint32_t b = a.block_lo + tile % a.n_blocks;
+    const uint32_t slice = tile / a.n_blocks;
+    const PlanBlock blk = a.blocks[b];
+    const uint32_t c0 = slice * W;
+    const uint32_t valid = min(uint32_t(W), a.row_words - c0);
+    const uint32_t vpad = (valid + 3u) & ~3u;
+
+    uint32_t bias_mask, zero_mask;
+    column_masks(a, c0, q0, q1, bias_mask, zero_mask);
+    for (uint32_t g = team; g < blk.n_groups; g += NTEAMS) {
+        const PlanGroup gr = a.groups[blk.group_begin + g];
+        uint32_t acc[G][8];
+#pragma unroll
+        for (int m = 0; m < G; ++m)
+#pragma unroll
+            for (int e = 0; e < 8; ++e) acc[m][e] = 0;
+        const PlanTerm *tp = a.terms + blk.term_begin + gr.term_begin;
+        for (uint32_t t = 0; t < gr.n_terms; ++t) {
+            const PlanTerm tm = tp[t];
+            const PlanSlot sl = a.slots[blk.slot_begin + tm.slot];
+            if (sl.row >= a.n_rows) {
+                report_error(a.err, kDevBadIndex);
+                continue;
+            }
+            const uint8_t *src = a.in + uint64_t(sl.row) * a.in_stride;
+            uint4 x0 = make_uint4(0, 0, 0, 0), x1 = make_uint4(0, 0, 0, 0);
+            if (sl.rot == 0) {
+                if (q0 < vpad) {
+                    const int4 v = ldg_nc_v4(src + (uint64_t(c0) + q0) * 4);
+                    x0 = make_uint4(uint32_t(v.x), uint32_t(v.y), uint32_t(v.z), uint32_t(v.w));
+                }
+                if (q1 < vpad) {
+                    const int4 v = ldg_nc_v4(src + (uint64_t(c0) + q1) * 4);
+                    x1 = make_uint4(uint32_t(v.x), uint32_t(v.y), uint32_t(v.z), uint32_t(v.w));
+                }
+            } else {
+                const uint32_t *s32 = reinterpret_cast<const uint32_t *>(src);
+                uint32_t tmp[8];
+#pragma unroll
+                for (int e = 0; e < 8; ++e) {
+                    const uint32_t q = e < 4 ? q0 + e : q1 + (e - 4);
+                    tmp[e] = q < valid ? rotated_word(s32, c0 + q, sl.rot, a.N) : 0u;
+                }
+                x0 = make_uint4(tmp[0], tmp[1], tmp[2], tmp[3]);
+                x1 = make_uint4(tmp[4], tmp[5], tmp[6], tmp[7]);
+            }
+            mac8<G>(acc, tm, x0, x1);
+        }
+        write_outputs<G>(a, gr, acc, c0, q0, q1, valid, bias_mask, zero_mask);
+    }
+}
+
+__global__ void k_finalize(const FinalizeArgs a) {
+    const uint64_t o = a.o_begin + uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (o >= a.o_end) return;
+    uint8_t *row = a.out_rows + (a.out_row_map ? uint64_t(a.out_row_map[o]) : o) * a.out_stride;
+    if (a.out_hdr_off >= 0) {
+        *reinterpret_cast<uint32_t *>(row + a.out_hdr_off) = a.out_index ? a.out_index[o] : uint32_t(o);
+        *reinterpret_cast<int32_t *>(row + a.out_hdr_off + 4) = a.tag;
+    }
+    if (a.out_var_off >= 0) {
+        // TFHE bookkeeping of tLweAddMulTo: variance += coef^2 * var_in, in
+        // CSR order, without contraction (matches the host's rounding).
+        double v = 0.0;
+        if (a.in_var_off >= 0) {
+            for (uint64_t t = a.var_ptr[o]; t < a.var_ptr[o + 1]; ++t) {
+                const int64_t c = a.var_coef[t];
+                const double vin =
+                    *reinterpret_cast<const double *>(a.in_rows + uint64_t(a.var_row[t]) * a.in_stride + a.in_var_off);
+                v = __dadd_rn(v, __dmul_rn(double(c * c), vin));
+            }
+        }
+        *reinterpret_cast<double *>(row + a.out_var_off) = v;
+    }
+}
+
+using KernelFn = void (*)(const ScoreArgs);
+
+template <int G>
+KernelFn pick(KernelKind kind, uint32_t w) {
+    const bool win = kind == KernelKind::kWindow;
+    switch (w) {
+        case 256: return win ? k_score_window<256, G> : k_score_direct<256, G>;
+        case 512: return win ? k_score_window<512, G> : k_score_direct<512, G>;
+        case 1024: return win ? k_score_window<1024, G> : k_score_direct<1024, G>;
+        case 2048: return win ? k_score_window<2048, G> : k_score_direct<2048, G>;
+        default: return nullptr;
+    }
+}
+
+KernelFn pick_kernel(KernelKind kind, uint32_t w, uint32_t g) {
+    return g == 1 ? pick<1>(kind, w) : g == 3 ? pick<3>(kind, w) : nullptr;
+}
+
+}  // namespace
+
+size_t window_smem_bytes(uint32_t slice_words, uint32_t max_slots, uint32_t max_terms, uint32_t max_groups) {
+    return 128 + size_t(max_slots) * slice_words * 4 + size_t(max_terms) * sizeof(PlanTerm) +
+           size_t(max_groups) * sizeof(PlanGroup);
+}
+
+cudaError_t configure_window_kernels(size_t max_smem) {
+    for (uint32_t w : {256u, 512u, 1024u, 2048u})
+        for (uint32_t g : {1u, 3u}) {
+            cudaError_t e = cudaFuncSetAttribute(pick_kernel(KernelKind::kWindow, w, g),
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, int(max_smem));
+            if (e != cudaSuccess) return e;
+        }
+    return cudaSuccess;
+}
+
+int window_ctas_per_sm(uint32_t slice_words, uint32_t group_size, size_t smem_bytes) {
+    KernelFn fn = pick_kernel(KernelKind::kWindow, slice_words, group_size);
+    if (!fn) return 0;
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, kThreads, smem_bytes) != cudaSuccess) return 0;
+    return n;
+}
+
+cudaError_t launch_score(KernelKind kind, uint32_t slice_words, uint32_t group_size, const ScoreArgs &a,
+                         uint32_t ctas, cudaStream_t stream) {
+    KernelFn fn = pick_kernel(kind, slice_words, group_size);
+    if (!fn) return cudaErrorInvalidValue;
+    if (a.n_tiles == 0) return cudaSuccess;
+    if (kind == KernelKind::kWindow) {
+        const size_t smem = window_smem_bytes(slice_words, a.max_slots, a.max_terms, a.max_groups);
+        cudaError_t e = cudaMemsetAsync(a.tile_counter, 0, sizeof(uint32_t), stream);
+        if (e != cudaSuccess) return e;
+        fn<<<ctas < a.n_tiles ? ctas : a.n_tiles, kThreads, smem, stream>>>(a);
+    } else {
+        fn<<<a.n_tiles, kThreads, 0, stream>>>(a);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_finalize(const FinalizeArgs &a, cudaStream_t stream) {
+    if (a.o_end <= a.o_begin || (a.out_var_off < 0 && a.out_hdr_off < 0)) return cudaSuccess;
+    const uint32_t threads = 256;
+    const uint64_t blocks = (a.o_end - a.o_begin + threads - 1) / threads;
+    k_finalize<<<uint32_t(blocks), threads, 0, stream>>>(a);
+    return cudaGetLastError();
+}
+
+}  // namespace idash

@@ -1,0 +1,73 @@
+// Launch-side view of the scoring kernels (score_kernels.cu).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "device_status.hpp"
+#include "plan.hpp"
+
+namespace idash {
+
+enum : uint32_t { kFormTrlwe = 0, kFormLwe = 1 };
+
+struct ScoreArgs {
+    const PlanBlock *blocks;
+    const PlanSlot *slots;
+    const PlanGroup *groups;
+    const PlanTerm *terms;
+    uint32_t block_lo, n_blocks;  // blocks [block_lo, block_lo + n_blocks)
+    uint32_t n_slices;            // column slices per row
+    uint32_t row_words;           // valid int32 words per row
+    uint32_t n_tiles;             // n_blocks * n_slices
+    uint32_t n_rows;              // input rows (bounds guard)
+    const uint8_t *in;            // coefficient 0 of input row 0
+    uint64_t in_stride;           // bytes
+    uint8_t *out;                 // coefficient 0 of output row 0
+    uint64_t out_stride;          // bytes
+    uint64_t out_lo, out_hi;      // outputs written: [out_lo, out_hi)
+    uint64_t out_row_base;        // output o goes to row (o - out_row_base) ...
+    const uint32_t *out_row_map;  // ... or to row out_row_map[o] when non-null
+    uint32_t form;                // kFormTrlwe / kFormLwe
+    uint32_t N, num_samples, region_size;  // TRLWE epilogue
+    uint32_t lwe_n1;                       // LWE: n + 1 words per sample
+    uint32_t max_slots, max_terms, max_groups;  // shared-memory carve-up
+    uint32_t *tile_counter;       // persistent kernel: next tile (zeroed before launch)
+    uint32_t *err;                // device error word
+};
+
+enum class KernelKind : int { kWindow = 0, kDirect = 1 };
+
+// Shared memory a window-kernel CTA needs for the given limits.
+size_t window_smem_bytes(uint32_t slice_words, uint32_t max_slots, uint32_t max_terms, uint32_t max_groups);
+
+// Launches one scoring kernel.  `ctas` is the persistent grid size (window
+// kernel) and is ignored by the direct kernel (one CTA per tile).
+cudaError_t launch_score(KernelKind kind, uint32_t slice_words, uint32_t group_size, const ScoreArgs &a,
+                         uint32_t ctas, cudaStream_t stream);
+
+// Allows every window-kernel instance up to `max_smem` bytes of dynamic
+// shared memory (once per context, before any launch or capture).
+cudaError_t configure_window_kernels(size_t max_smem);
+
+// Largest resident CTA count per SM for the window kernel at this smem size.
+int window_ctas_per_sm(uint32_t slice_words, uint32_t group_size, size_t smem_bytes);
+
+struct FinalizeArgs {
+    const uint64_t *var_ptr;
+    const uint32_t *var_row;
+    const int32_t *var_coef;
+    const uint32_t *out_index;  // may be null: index = o
+    const uint32_t *out_row_map;  // may be null: row = o
+    uint64_t o_begin, o_end;    // outputs finalised: [o_begin, o_end)
+    const uint8_t *in_rows;     // input row 0 start (record start, not payload)
+    uint64_t in_stride;
+    int64_t in_var_off;         // -1: inputs carry no variance (outputs get 0)
+    uint8_t *out_rows;          // output row 0 start
+    uint64_t out_stride;
+    int64_t out_var_off, out_hdr_off;
+    int32_t tag;
+};
+cudaError_t launch_finalize(const FinalizeArgs &a, cudaStream_t stream);
+
+}  // namespace idash

@@ -1,0 +1,241 @@
+/*
+ * idash_gpu.h — C ABI of the GB300 party-B scoring library (libidash_gpu.so).
+ *
+ * The library replaces the reference's cloud step,
+ *   void cloud_compute_score(EncryptedPredictions&, const EncryptedData&,
+ *                            const Model&, const IdashParams&)
+ * (eval/idash.h:251-252, defined at eval/idash.cpp:763-848, called once from
+ * eval/cloud.cpp:17), with hand-written sm_103a CUDA behind plain C entry
+ * points: no C++ or torch types cross this boundary, every function returns an
+ * idash_status and none aborts (the reference aborts through
+ * REQUIRE_DRAMATICALLY, eval/idash.h:12).
+ *
+ * Vocabulary (the reference's):
+ *   input feature   FeatBigIndex of a tag SNP's one-hot bit (eval/idash.h:40)
+ *   FeatIndex       which TRLWE holds the feature: bidx / NUM_REGIONS (eval/idash.h:87)
+ *   region          bidx % NUM_REGIONS: the slot block [r*REGION_SIZE, ...) (eval/idash.h:89)
+ *   output          one (target position, genotype) model; FeatBigIndex out (eval/idash.h:129-134)
+ *   constant        the model's "Constant" entry, feature 0xFFFFFFFF (eval/idash.h:93)
+ * All ciphertext arithmetic is on Torus32 = Z/2^32 with wrap-around.
+ */
+#ifndef IDASH_GPU_H
+#define IDASH_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define IDASH_GPU_ABI_VERSION 1
+#define IDASH_CONSTANT_FEATURE 0xFFFFFFFFu
+
+typedef enum {
+    IDASH_OK = 0,
+    IDASH_ERR_INVALID_ARGUMENT = 1, /* bad size, pointer, alignment or parameter */
+    IDASH_ERR_CUDA = 2,             /* a CUDA runtime call failed (see idash_last_error) */
+    IDASH_ERR_OUT_OF_MEMORY = 3,    /* device or pinned-host allocation failed */
+    IDASH_ERR_INDEX = 4,            /* a model term names a feature with no input ciphertext
+                                       (the reference aborts here: eval/idash.h:164) */
+    IDASH_ERR_DEVICE_TIMEOUT = 5,   /* a bounded device-side wait expired; results invalid */
+    IDASH_ERR_IO = 6,               /* file could not be opened, read or written */
+    IDASH_ERR_FORMAT = 7,           /* malformed params.bin / model / ciphertext file */
+    IDASH_ERR_UNSUPPORTED = 8,      /* parameter outside what the kernels implement (k != 1 ...) */
+    IDASH_ERR_ADMISSION = 9,        /* serving: request can never fit the HBM budget */
+    IDASH_ERR_STATE = 10            /* call out of order (e.g. score before a model is loaded) */
+} idash_status;
+
+typedef struct idash_ctx idash_ctx;     /* one device, one stream, scratch, error word */
+typedef struct idash_model idash_model; /* a resident, planned model (one layout) */
+
+/* ---------------------------------------------------------------- context */
+const char *idash_status_string(idash_status s);
+int idash_abi_version(void);
+
+/* Opens `device` and creates the context's stream.  Replaces nothing in the
+ * reference (its only "context" is the OpenMP team, eval/idash.cpp:779). */
+idash_status idash_open(idash_ctx **ctx, int device);
+void idash_close(idash_ctx *ctx);
+/* Human-readable detail of the last failure on this context ("" if none);
+ * with ctx == NULL, why the last idash_open on this thread failed. */
+const char *idash_last_error(const idash_ctx *ctx);
+/* The context's CUDA stream (a cudaStream_t), for callers that order work on it. */
+void *idash_stream(idash_ctx *ctx);
+/* Blocks until the context's stream is idle, then reads and clears the device
+ * error word.  Returns IDASH_ERR_DEVICE_TIMEOUT / IDASH_ERR_INDEX if a kernel
+ * reported one since the last check. */
+idash_status idash_sync(idash_ctx *ctx);
+
+/* Tunables: "kernel" (0 batched persistent window kernel, 1 plain per-output
+ * kernel), "slice_words" (0 = autotune), "ctas_per_sm", "graph" (0/1: replay
+ * launches from a CUDA graph), "max_window_slots", "max_group_terms". */
+idash_status idash_set_option(idash_ctx *ctx, const char *name, int64_t value);
+idash_status idash_get_option(const idash_ctx *ctx, const char *name, int64_t *value);
+
+typedef struct {
+    uint64_t kernel_launches;   /* scoring kernels launched by this context */
+    uint64_t graph_launches;    /* CUDA-graph replays */
+    uint64_t h2d_bytes, d2h_bytes;
+} idash_stats;
+idash_status idash_get_stats(const idash_ctx *ctx, idash_stats *out);
+
+/* ------------------------------------------------------------ memory helpers
+ * Device and page-locked host buffers owned by the caller (freed with the
+ * matching *_free).  Copies are ordered on the context's stream. */
+idash_status idash_device_alloc(idash_ctx *ctx, size_t bytes, void **ptr);
+idash_status idash_device_free(idash_ctx *ctx, void *ptr);
+idash_status idash_host_alloc(idash_ctx *ctx, size_t bytes, void **ptr);
+idash_status idash_host_free(idash_ctx *ctx, void *ptr);
+idash_status idash_copy_h2d(idash_ctx *ctx, void *dst, const void *src, size_t bytes);
+idash_status idash_copy_d2h(idash_ctx *ctx, void *dst, const void *src, size_t bytes);
+idash_status idash_memset_device(idash_ctx *ctx, void *dst, int value, size_t bytes);
+
+/* ------------------------------------------------------------- row layouts
+ * Ciphertexts live in rows.  A TRLWE row (k = 1) is 2N int32 coefficients:
+ * the mask a[0..N) then the body b[0..N).  A row may sit inside a larger
+ * record, e.g. one entry of encrypted_data.bin / encrypted_prediction.bin
+ * (eval/idash.cpp:540-556, :596-613):
+ *   uint32 FeatIndex/FeatBigIndex | int32 record tag | 2N int32 | double variance
+ * which is 8208 bytes: layout {8208, 8, 8200, 0} with `base` = file image + 8. */
+typedef struct {
+    uint64_t row_stride;     /* bytes between consecutive rows; multiple of 16 */
+    uint64_t payload_offset; /* bytes from row start to coefficient 0; base+offset 16-byte aligned */
+    int64_t variance_offset; /* bytes to the double current_variance, or -1 */
+    int64_t header_offset;   /* outputs: bytes to (uint32 index, int32 tag), or -1 */
+} idash_row_layout;
+
+/* ------------------------------------------- TRLWE-packed scoring (drop-in)
+ * Parameters of IdashParams that the scoring step reads (eval/idash.h:45-80,
+ * eval/idash.cpp:766-770). */
+typedef struct {
+    uint32_t N;           /* TRLWE polynomial size, IdashParams::N (1024) */
+    uint32_t k;           /* must be 1 (eval/idash.cpp:768) */
+    uint32_t num_samples; /* NUM_SAMPLES: individuals packed per region */
+    uint32_t num_regions; /* NUM_REGIONS */
+    uint32_t region_size; /* REGION_SIZE; num_regions*region_size <= N */
+    int32_t one_t32;      /* ONE_IN_T32 = dtot32(2^-14) = 2^18 (eval/idash.cpp:39) */
+    int32_t record_tag;   /* tag written into output record headers */
+} idash_trlwe_params;
+
+/* Loads a Model (eval/idash.h:129-134) flattened to CSR and plans it for the
+ * device: output o's terms are term_feat/term_coef[term_ptr[o] .. term_ptr[o+1]),
+ * in the order the caller iterates the model (that order only matters for the
+ * double variance bookkeeping).  Outputs should be numbered so that
+ * neighbouring targets are adjacent (FeatBigIndex order is): consecutive
+ * outputs share input windows.  out_index[o] is the output's FeatBigIndex,
+ * written into record headers (NULL: o).  out_row[o] is the output row that
+ * receives output o (NULL: row o; must be a permutation of [0, n_out)); the
+ * host-memory path requires NULL.  in_row_of_index maps FeatIndex to the
+ * input row that holds it (NULL: identity); n_in_rows bounds it.
+ * Replaces the setup half of cloud_compute_score (eval/idash.cpp:772-777). */
+idash_status idash_model_trlwe(idash_ctx *ctx, idash_model **model, const idash_trlwe_params *params,
+                               uint64_t n_out, const uint32_t *out_index, const uint32_t *out_row,
+                               const uint64_t *term_ptr, const uint32_t *term_feat, const int32_t *term_coef,
+                               uint64_t n_in_index, const uint32_t *in_row_of_index, uint64_t n_in_rows);
+
+/* Scores every output of a TRLWE model: the hot loop of cloud_compute_score
+ * (eval/idash.cpp:779-842).  d_in / d_out are device pointers to row 0 of the
+ * input and output rows; output o goes to row o.  Asynchronous on `stream`
+ * (NULL = the context's stream). */
+idash_status idash_score_trlwe_device(idash_model *model, const void *d_in, const idash_row_layout *in_layout,
+                                      void *d_out, const idash_row_layout *out_layout, void *stream);
+
+/* Same, end to end from host memory: copies the input rows in, scores, and
+ * copies the output rows back, overlapping the copies with the kernels in
+ * chunks.  Host buffers should be page-locked (idash_host_alloc).  Returns
+ * after the outputs are in h_out. */
+idash_status idash_score_trlwe_host(idash_model *model, const void *h_in, const idash_row_layout *in_layout,
+                                    uint64_t n_in_rows, void *h_out, const idash_row_layout *out_layout);
+
+/* ------------------------------------------- per-individual LWE scoring
+ * Each individual's one-hot bit is its own LWE sample (n mask words + body).
+ * Input row f holds n_indiv samples of (n+1) int32, row stride in words a
+ * multiple of 4.  Output o, row (o - out_begin) of d_out, same layout.  The
+ * result for individual i equals SampleExtract_i of the TRLWE form. */
+typedef struct {
+    uint32_t n;       /* LWE dimension (1024) */
+    uint32_t n_indiv; /* individuals per row */
+    int32_t one_t32;  /* constant scaling (2^18) */
+} idash_lwe_params;
+
+idash_status idash_model_lwe(idash_ctx *ctx, idash_model **model, const idash_lwe_params *params,
+                             uint64_t n_out, const uint64_t *term_ptr, const uint32_t *term_feat,
+                             const int32_t *term_coef, uint64_t n_feat_rows);
+/* Scores outputs [out_begin, out_end) (any range; outputs beyond HBM are
+ * produced range by range).  n_indiv may be smaller than the model's (serving
+ * requests of fewer individuals); strides are in int32 words. */
+idash_status idash_score_lwe_device(idash_model *model, uint32_t n_indiv, const int32_t *d_in,
+                                    uint64_t in_row_stride, uint64_t out_begin, uint64_t out_end,
+                                    int32_t *d_out, uint64_t out_row_stride, void *stream);
+
+/* Model facts: outputs, total terms, planned blocks, slice width chosen. */
+typedef struct {
+    uint64_t n_out, n_terms, n_groups, n_blocks, n_slots;
+    uint32_t slice_words, max_window_slots, kernel;
+    uint64_t algorithmic_in_rows; /* distinct input rows the model reads */
+} idash_model_info;
+idash_status idash_model_get_info(const idash_model *model, idash_model_info *info);
+/* Re-plans the model for a new kernel / slice choice (after idash_set_option). */
+idash_status idash_model_replan(idash_model *model);
+void idash_model_free(idash_model *model);
+
+/* ------------------------------------------- the cloud step on files
+ * eval/cloud.cpp:3-28 as one call: reads params.bin (eval/idash.cpp:200-261),
+ * the model directory of <pos>_<snp>.hr files (eval/idash.cpp:66-114) and
+ * encrypted_data.bin (:513-535), scores on `device`, and writes
+ * encrypted_prediction.bin (:596-613) with the records in the order the
+ * reference writes them.  Ciphertext files move as single bulk images. */
+typedef struct {
+    double read_s;   /* params + model + ciphertext file reads */
+    double plan_s;   /* model flattening and device planning */
+    double score_s;  /* host->device copy, kernels, device->host copy */
+    double write_s;  /* prediction file write */
+    uint64_t n_in_records, n_out_records;
+} idash_cloud_report;
+idash_status idash_cloud_files(int device, const char *params_file, const char *model_dir, const char *data_file,
+                               const char *pred_file, idash_cloud_report *report, char *errbuf, size_t errbuf_len);
+
+/* ------------------------------------------- synthetic workloads (host)
+ * Seeded synthetic imputation models with the reference's shapes: tag SNPs at
+ * sorted positions, targets at sorted random positions, each target's
+ * neighbours = its k nearest tags (train/to_vw.py:33-34), 3 outputs per target
+ * with coefficients uniform in [-8192, 8191] (zeros dropped,
+ * train/test_vw_hr.py:44) and an integer bias.  Features are numbered as the
+ * reference's keygen numbers them: tag p owns 3p, 3p+1, 3p+2
+ * (eval/idash.cpp:388-390); target t owns outputs 3t..3t+2 (:337-339). */
+typedef struct {
+    uint64_t seed;
+    uint32_t n_tags, n_targets;
+    uint32_t neighbours;          /* fixed neighbour count, or 0 to draw from choices[] */
+    uint32_t n_choices;
+    uint32_t choices[8];          /* e.g. {5,10,20,30,50} */
+} idash_synth_spec;
+
+typedef struct {
+    uint64_t n_out, n_terms;
+    uint64_t *term_ptr;     /* n_out + 1 */
+    uint32_t *term_feat;    /* n_terms */
+    int32_t *term_coef;     /* n_terms */
+    uint64_t *tag_pos;      /* n_tags positions (sorted) */
+    uint64_t *target_pos;   /* n_targets positions (sorted) */
+    uint32_t *window_start; /* per target: first neighbour tag */
+    uint32_t *window_len;   /* per target: neighbour count */
+} idash_synth_model_t;
+
+idash_status idash_synth_model(const idash_synth_spec *spec, idash_synth_model_t *out);
+void idash_synth_model_free(idash_synth_model_t *m);
+
+/* Device generators of synthetic ciphertexts (valid encryptions under a
+ * seeded binary key, one-hot genotypes, noise sd ~2^-25): per-individual LWE
+ * rows, and TRLWE rows packing num_samples individuals per region. */
+idash_status idash_synth_lwe_device(idash_ctx *ctx, uint64_t seed, uint32_t n, uint32_t n_indiv,
+                                    uint64_t n_feat_rows, int32_t *d_out, uint64_t row_stride, void *stream);
+idash_status idash_synth_trlwe_device(idash_ctx *ctx, uint64_t seed, const idash_trlwe_params *params,
+                                      uint32_t n_tags, void *d_out, const idash_row_layout *layout, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,201 @@
+/*
+ * oracle.c — TEST INFRASTRUCTURE ONLY (see oracle.h).  Plain C + OpenMP.
+ *
+ * oracle_trlwe_score restates cloud_compute_score (eval/idash.cpp:763-848)
+ * step by step on flat arrays; the TFHE primitives it calls there are
+ * restated inline from their definitions:
+ *   tLweClear (idash.cpp:796)       -> zero a and b, variance = 0
+ *   tLweAddMulTo (idash.cpp:817)    -> a,b += coef * C; variance += coef^2 var
+ *   tLweCopy (idash.cpp:825)        -> copy coefficients and variance
+ *   torusPolynomialMulByXai (:832)  -> negacyclic rotation by X^e, e in [0,2N)
+ *   tLweAddTo (idash.cpp:835)       -> a,b += rotated; variance += 0
+ */
+#include "oracle.h"
+
+#include <omp.h>
+#include <stdlib.h>
+#include <string.h>
+
+uint64_t oracle_mix64(uint64_t z) {
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+uint32_t oracle_hash32(uint64_t seed, uint64_t stream, uint64_t index) {
+    const uint64_t key = oracle_mix64(seed + oracle_mix64(stream));
+    return (uint32_t)(oracle_mix64(key ^ index) >> 32);
+}
+
+static inline void rotate_add(uint32_t *acc, const uint32_t *src, uint32_t N, uint32_t e) {
+    /* acc += X^e * src mod X^N+1, e in [0, 2N) */
+    for (uint32_t j = 0; j < N; ++j) {
+        uint32_t t = j + e;
+        int neg = 0;
+        if (t >= 2 * N) t -= 2 * N;
+        if (t >= N) { t -= N; neg = 1; }
+        acc[t] += neg ? 0u - src[j] : src[j];
+    }
+}
+
+int oracle_trlwe_score(uint32_t N, uint32_t num_samples, uint32_t num_regions, uint32_t region_size,
+                       int32_t one_t32, uint64_t n_out, const uint64_t *term_ptr, const uint32_t *term_feat,
+                       const int32_t *term_coef, const uint32_t *row_of_index, uint64_t n_index,
+                       uint64_t n_rows, const int32_t *in_rows, const double *in_var,
+                       int32_t *out_rows, double *out_var, int n_threads) {
+    if (N == 0 || num_regions == 0 || region_size == 0 || num_samples > region_size ||
+        (uint64_t)num_regions * region_size > N)
+        return -1;
+    const uint64_t W = 2ull * N; /* k = 1: a then b */
+    int bad = 0;
+    if (n_threads <= 0) n_threads = omp_get_max_threads();
+#pragma omp parallel num_threads(n_threads) reduction(| : bad)
+    {
+        uint32_t *tmp = (uint32_t *)calloc((size_t)num_regions * W, sizeof(uint32_t));
+        double *tvar = (double *)calloc(num_regions, sizeof(double));
+#pragma omp for schedule(dynamic, 64)
+        for (int64_t o = 0; o < (int64_t)n_out; ++o) {
+            memset(tmp, 0, sizeof(uint32_t) * num_regions * W);
+            memset(tvar, 0, sizeof(double) * num_regions);
+            for (uint64_t t = term_ptr[o]; t < term_ptr[o + 1]; ++t) {
+                const uint32_t feat = term_feat[t];
+                const uint32_t coef = (uint32_t)term_coef[t];
+                if (feat == ORACLE_CONSTANT_FEATURE) {
+                    const uint32_t scaled = coef * (uint32_t)one_t32;
+                    for (uint32_t s = 0; s < num_samples; ++s) tmp[N + s] += scaled;
+                    continue;
+                }
+                const uint32_t region = feat % num_regions;
+                const uint64_t index = feat / num_regions;
+                uint64_t row = index;
+                if (row_of_index) {
+                    if (index >= n_index) { bad = 1; continue; }
+                    row = row_of_index[index];
+                }
+                if (row >= n_rows) { bad = 1; continue; }
+                const uint32_t *src = (const uint32_t *)(in_rows + row * W);
+                uint32_t *dst = tmp + (uint64_t)region * W;
+                for (uint64_t j = 0; j < W; ++j) dst[j] += coef * src[j];
+                if (in_var) tvar[region] += (double)((int64_t)term_coef[t] * term_coef[t]) * in_var[row];
+            }
+            uint32_t *out = (uint32_t *)(out_rows + (uint64_t)o * W);
+            memcpy(out, tmp, sizeof(uint32_t) * W);
+            for (uint32_t r = 1; r < num_regions; ++r) {
+                const uint32_t e = 2 * N - r * region_size;
+                rotate_add(out, tmp + (uint64_t)r * W, N, e);          /* mask a */
+                rotate_add(out + N, tmp + (uint64_t)r * W + N, N, e);  /* body b */
+            }
+            for (uint32_t j = region_size; j < N; ++j) out[N + j] = 0;
+            if (out_var) out_var[o] = tvar[0];
+        }
+        free(tmp);
+        free(tvar);
+    }
+    return bad ? -2 : 0;
+}
+
+int oracle_lwe_score(uint32_t n, uint32_t n_indiv, int32_t one_t32, uint64_t n_out,
+                     const uint64_t *term_ptr, const uint32_t *term_feat, const int32_t *term_coef,
+                     uint64_t n_feat_rows, const int32_t *in, uint64_t in_row_stride,
+                     uint64_t out_begin, uint64_t out_end, int32_t *out, uint64_t out_row_stride,
+                     int n_threads) {
+    if (out_end > n_out || out_begin > out_end) return -1;
+    const uint64_t L = (uint64_t)n_indiv * (n + 1);
+    int bad = 0;
+    if (n_threads <= 0) n_threads = omp_get_max_threads();
+#pragma omp parallel for num_threads(n_threads) schedule(dynamic, 4) reduction(| : bad)
+    for (int64_t o = (int64_t)out_begin; o < (int64_t)out_end; ++o) {
+        uint32_t *dst = (uint32_t *)(out + (uint64_t)(o - (int64_t)out_begin) * out_row_stride);
+        memset(dst, 0, sizeof(uint32_t) * L);
+        for (uint64_t t = term_ptr[o]; t < term_ptr[o + 1]; ++t) {
+            const uint32_t feat = term_feat[t];
+            const uint32_t coef = (uint32_t)term_coef[t];
+            if (feat == ORACLE_CONSTANT_FEATURE) {
+                const uint32_t scaled = coef * (uint32_t)one_t32;
+                for (uint32_t i = 0; i < n_indiv; ++i) dst[(uint64_t)i * (n + 1) + n] += scaled;
+                continue;
+            }
+            if (feat >= n_feat_rows) { bad = 1; continue; }
+            const uint32_t *src = (const uint32_t *)(in + (uint64_t)feat * in_row_stride);
+            for (uint64_t j = 0; j < L; ++j) dst[j] += coef * src[j];
+        }
+    }
+    return bad ? -2 : 0;
+}
+
+int oracle_intpoly_score(uint32_t N, uint32_t num_samples, uint32_t region_size, int32_t one_t32,
+                         uint64_t n_out, const uint64_t *term_ptr, const uint32_t *term_feat,
+                         const int16_t *term_poly, const int32_t *bias, uint64_t n_rows,
+                         const int32_t *in_rows, uint64_t out_begin, uint64_t out_end,
+                         int32_t *out_rows, int n_threads) {
+    if (out_end > n_out || out_begin > out_end || num_samples > region_size || region_size > N) return -1;
+    const uint64_t W = 2ull * N;
+    int bad = 0;
+    if (n_threads <= 0) n_threads = omp_get_max_threads();
+#pragma omp parallel for num_threads(n_threads) schedule(dynamic, 1) reduction(| : bad)
+    for (int64_t o = (int64_t)out_begin; o < (int64_t)out_end; ++o) {
+        uint32_t *dst = (uint32_t *)(out_rows + (uint64_t)(o - (int64_t)out_begin) * W);
+        memset(dst, 0, sizeof(uint32_t) * W);
+        for (uint64_t t = term_ptr[o]; t < term_ptr[o + 1]; ++t) {
+            const uint32_t feat = term_feat[t];
+            if (feat >= n_rows) { bad = 1; continue; }
+            const int16_t *w = term_poly + t * N;
+            for (uint32_t p = 0; p < 2; ++p) {
+                const uint32_t *c = (const uint32_t *)(in_rows + (uint64_t)feat * W + (uint64_t)p * N);
+                uint32_t *d = dst + (uint64_t)p * N;
+                for (uint32_t i = 0; i < N; ++i) {
+                    const uint32_t wi = (uint32_t)(int32_t)w[i];
+                    if (wi == 0) continue;
+                    for (uint32_t j = 0; j < N; ++j) {
+                        const uint32_t prod = wi * c[j];
+                        const uint32_t k = i + j;
+                        if (k < N) d[k] += prod;
+                        else d[k - N] -= prod; /* X^N = -1 */
+                    }
+                }
+            }
+        }
+        const uint32_t scaled = (uint32_t)bias[o] * (uint32_t)one_t32;
+        for (uint32_t s = 0; s < num_samples; ++s) dst[N + s] += scaled;
+        for (uint32_t j = region_size; j < N; ++j) dst[N + j] = 0;
+    }
+    return bad ? -2 : 0;
+}
+
+void oracle_sample_extract(uint32_t N, const int32_t *trlwe, uint32_t slot, int32_t *out) {
+    const uint32_t *a = (const uint32_t *)trlwe;
+    for (uint32_t j = 0; j < N; ++j) {
+        if (j <= slot) out[j] = (int32_t)a[slot - j];
+        else out[j] = (int32_t)(0u - a[N + slot - j]);
+    }
+    out[N] = trlwe[N + slot];
+}
+
+/* Synthetic per-individual LWE inputs (streams as in the product generator):
+ *   key bit s_j      = hash(seed, 1, j) & 1
+ *   genotype g(p,i)  = hash(seed, 2, p*n_indiv + i) % 3, feature f = 3p+v has bit (g == v)
+ *   mask a_j(f,i)    = hash(seed, 3, (f*n_indiv + i)*n + j)
+ *   noise e(f,i)     = sum_{k<4} (hash(seed, 4, (f*n_indiv+i)*4+k) % 221) - 440
+ *   body b(f,i)      = sum_j a_j s_j + e + bit * 2^18   (mod 2^32)
+ * Word w of row f is individual w/(n+1), position w%(n+1) (n = body). */
+void oracle_synth_lwe_words(uint64_t seed, uint32_t n, uint32_t n_indiv, uint64_t feature,
+                            uint64_t w0, uint64_t count, int32_t *out) {
+    for (uint64_t w = w0; w < w0 + count; ++w) {
+        const uint64_t i = w / (n + 1), j = w % (n + 1);
+        const uint64_t sample = feature * n_indiv + i;
+        if (j < n) {
+            out[w - w0] = (int32_t)oracle_hash32(seed, 3, sample * n + j);
+            continue;
+        }
+        uint32_t b = 0;
+        for (uint32_t k = 0; k < n; ++k)
+            if (oracle_hash32(seed, 1, k) & 1u) b += oracle_hash32(seed, 3, sample * n + k);
+        for (uint32_t k = 0; k < 4; ++k) b += (oracle_hash32(seed, 4, sample * 4 + k) % 221u);
+        b -= 440u;
+        const uint64_t p = feature / 3, v = feature % 3;
+        const uint32_t g = oracle_hash32(seed, 2, p * n_indiv + i) % 3u;
+        if (g == v) b += 1u << 18;
+        out[w - w0] = (int32_t)b;
+    }
+}

@@ -1,0 +1,79 @@
+"""CPU-only checks of the C ABI library: it loads, exports every function the
+header declares, reports errors as statuses without a GPU, and its host-side
+synthetic model generator follows the reference's conventions."""
+import numpy as np
+import pytest
+
+_lib = pytest.importorskip("idash2019_2_gb300._lib")
+
+
+@pytest.fixture(scope="module")
+def lib():
+    try:
+        return _lib.load()
+    except ImportError as e:
+        pytest.skip(str(e))
+
+
+def test_library_exports_every_declared_function(lib):
+    declared = _lib.declared_functions()
+    assert len(declared) >= 25
+    for name in declared:
+        assert hasattr(lib, name), f"libidash_gpu.so does not export {name}"
+        assert name in _lib.PROTOTYPES, f"no ctypes prototype for {name}"
+    assert lib.idash_abi_version() == 1
+
+
+def test_status_strings(lib):
+    for code in range(11):
+        assert lib.idash_status_string(code)
+
+
+def test_open_without_device_is_a_status(lib):
+    import ctypes as C
+    h = C.c_void_p()
+    code = lib.idash_open(C.byref(h), 999)
+    assert code != 0
+    assert not h.value
+    assert lib.idash_last_error(None)
+
+
+def test_synth_model_windows_are_nearest_tags():
+    from idash2019_2_gb300 import gpu
+    w = gpu.synth_model(seed=42, n_tags=200, n_targets=500, choices=[5, 10, 20, 30, 50])
+    tags = w.tag_pos.astype(np.int64)
+    assert np.all(np.diff(tags) > 0)
+    assert np.all(np.diff(w.target_pos.astype(np.int64)) >= 0)
+    assert set(np.unique(w.window_len)) <= {5, 10, 20, 30, 50}
+    for t in range(0, 500, 37):
+        s, k = int(w.window_start[t]), int(w.window_len[t])
+        d = np.abs(tags - int(w.target_pos[t]))
+        inside = d[s:s + k].max()
+        outside = np.concatenate([d[:s], d[s + k:]])
+        assert outside.size == 0 or inside <= outside.min()
+    csr = w.model
+    assert csr.n_out == 1500
+    for o in range(0, csr.n_out, 101):
+        f = csr.term_feat[csr.term_ptr[o]:csr.term_ptr[o + 1]]
+        c = csr.term_coef[csr.term_ptr[o]:csr.term_ptr[o + 1]]
+        assert f[-1] == 0xFFFFFFFF
+        t = o // 3
+        tags_used = set((f[:-1] // 3).tolist())
+        assert tags_used <= set(range(int(w.window_start[t]), int(w.window_start[t] + w.window_len[t])))
+        assert np.all(c[:-1] != 0) and np.all(c >= -8192) and np.all(c <= 8191)
+
+
+def test_synth_model_is_deterministic():
+    from idash2019_2_gb300 import gpu
+    a = gpu.synth_model(seed=5, n_tags=50, n_targets=60, neighbours=5)
+    b = gpu.synth_model(seed=5, n_tags=50, n_targets=60, neighbours=5)
+    np.testing.assert_array_equal(a.model.term_coef, b.model.term_coef)
+    np.testing.assert_array_equal(a.model.term_feat, b.model.term_feat)
+
+
+def test_synth_model_rejects_bad_spec(lib):
+    import ctypes as C
+    spec = _lib.SynthSpec()
+    spec.n_tags = 0
+    m = _lib.SynthModel()
+    assert lib.idash_synth_model(C.byref(spec), C.byref(m)) == 1

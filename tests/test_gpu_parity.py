@@ -1,0 +1,254 @@
+"""GPU parity: the CUDA path (through the C ABI) against the reference's own
+outputs and the oracle, bit for bit.  Run on a GB300 after build()."""
+import filecmp
+import hashlib
+import json
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, ROOT, SMALL_CASES
+
+pytestmark = pytest.mark.gpu
+
+gpu = pytest.importorskip("idash2019_2_gb300.gpu")
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    c = gpu.Context(0)
+    yield c
+    c.close()
+
+
+def copy_case(name, dst):
+    src = os.path.join(GOLDEN, name)
+    for f in ["params.bin", "encrypted_data.bin"]:
+        shutil.copy(os.path.join(src, f), dst / f)
+    shutil.copytree(os.path.join(src, "model"), dst / "model")
+    return src
+
+
+@pytest.mark.parametrize("name", SMALL_CASES)
+def test_cloud_files_byte_identical_to_reference(tmp_path, name):
+    """The whole cloud step on the reference's own fixture files writes an
+    encrypted_prediction.bin identical byte for byte to the reference's."""
+    src = copy_case(name, tmp_path)
+    rep = gpu.cloud_files(str(tmp_path / "params.bin"), str(tmp_path / "model"), str(tmp_path / "encrypted_data.bin"),
+                          str(tmp_path / "encrypted_prediction.bin"))
+    assert rep["n_out_records"] > 0
+    assert filecmp.cmp(tmp_path / "encrypted_prediction.bin", os.path.join(src, "encrypted_prediction.bin"),
+                       shallow=False)
+
+
+@pytest.mark.parametrize("name", ["rand_r1_i1000", "rand_r4_i250", "rand_r10_i100"])
+def test_cloud_files_hash_pinned_medium(tmp_path, name):
+    import gen_inputs
+    meta = json.load(open(os.path.join(GOLDEN, "hashes.json")))[name]
+    gen_inputs.write_random_case(str(tmp_path), **{k: meta[k] for k in
+                                                  ("seed", "n_indiv", "n_tags", "n_targets", "neighbours")})
+    gpu.cloud_files(str(tmp_path / "params.bin"), str(tmp_path / "model"), str(tmp_path / "encrypted_data.bin"),
+                    str(tmp_path / "encrypted_prediction.bin"))
+    raw = open(tmp_path / "encrypted_prediction.bin", "rb").read()
+    assert len(raw) == meta["bytes"]
+    assert hashlib.sha256(raw).hexdigest() == meta["sha256"]
+
+
+def test_cloud_cli_matches_reference(tmp_path):
+    src = copy_case("ref_r10", tmp_path)
+    cli = os.path.join(ROOT, "idash2019_2_gb300", "idash_cloud")
+    r = subprocess.run([cli, "model"], cwd=tmp_path, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "fhe wall time (seconds)" in r.stdout and "BENCHMARK" in r.stdout
+    assert filecmp.cmp(tmp_path / "encrypted_prediction.bin", os.path.join(src, "encrypted_prediction.bin"),
+                       shallow=False)
+
+
+def random_rows(seed, n_rows, n=1024):
+    rng = np.random.default_rng(seed)
+    return rng.integers(0, 2 ** 32, size=(n_rows, 2 * n), dtype=np.uint64).astype(np.uint32).view(np.int32)
+
+
+@pytest.mark.parametrize("regions", [1, 3, 10])
+@pytest.mark.parametrize("kernel", [0, 1])
+def test_trlwe_synth_vs_oracle(ctx, oracle, regions, kernel):
+    num_samples = 1024 // regions - 1 if regions > 1 else 1000
+    region_size = 1024 // regions
+    w = gpu.synth_model(seed=7 + regions, n_tags=150, n_targets=400, neighbours=5)
+    n_rows = (3 * 150 + regions - 1) // regions
+    rows = random_rows(regions, n_rows)
+    ctx.set_option("kernel", kernel)
+    try:
+        m = gpu.TrlweModel(ctx, w.model, n_rows, num_samples, regions, region_size)
+        got = m.score(rows)
+        m.free()
+    finally:
+        ctx.set_option("kernel", 0)
+    want, _ = oracle.trlwe_score(w.model.term_ptr, w.model.term_feat, w.model.term_coef, rows, num_samples,
+                                 regions, region_size)
+    np.testing.assert_array_equal(got, want)
+
+
+@pytest.mark.parametrize("slice_words", [256, 512, 1024, 2048])
+@pytest.mark.parametrize("graph", [0, 1])
+def test_trlwe_device_path_tiles(ctx, oracle, slice_words, graph):
+    """Every slice width of the window kernel, with and without graph replay,
+    on the device-resident path (dense rows)."""
+    w = gpu.synth_model(seed=3, n_tags=200, n_targets=700, choices=[5, 10, 20, 30, 50])
+    n_rows = 600
+    rows = random_rows(5, n_rows)
+    ctx.set_option("slice_words", slice_words)
+    ctx.set_option("graph", graph)
+    try:
+        m = gpu.TrlweModel(ctx, w.model, n_rows, 1000, 1, 1024)
+        d_in = ctx.device_alloc(rows.nbytes)
+        d_out = ctx.device_alloc(m.n_out * 8192)
+        d_in.upload(rows)
+        for _ in range(2):  # second call replays the graph
+            d_out.zero()
+            m.score_device(d_in.ptr, gpu.DENSE_TRLWE, d_out.ptr, gpu.DENSE_TRLWE)
+            ctx.sync()
+            got = d_out.download(dtype=np.int32).reshape(m.n_out, 2048)
+            want, _ = oracle.trlwe_score(w.model.term_ptr, w.model.term_feat, w.model.term_coef, rows, 1000, 1,
+                                         1024)
+            np.testing.assert_array_equal(got, want)
+        assert m.info()["slice_words"] == slice_words
+        m.free()
+    finally:
+        ctx.set_option("slice_words", 0)
+        ctx.set_option("graph", 1)
+
+
+def test_trlwe_autotune_picks_a_correct_plan(ctx, oracle):
+    w = gpu.synth_model(seed=4, n_tags=300, n_targets=1500, neighbours=5)
+    rows = random_rows(6, 900)
+    m = gpu.TrlweModel(ctx, w.model, 900, 1000, 1, 1024)
+    got = m.score(rows)  # first call autotunes
+    got2 = m.score(rows)
+    want, _ = oracle.trlwe_score(w.model.term_ptr, w.model.term_feat, w.model.term_coef, rows, 1000, 1, 1024)
+    np.testing.assert_array_equal(got, want)
+    np.testing.assert_array_equal(got2, want)
+    info = m.info()
+    assert info["kernel"] == 0 and info["slice_words"] in (512, 1024, 2048)
+
+
+def test_lwe_vs_oracle_ranges(ctx, oracle):
+    n, n_indiv, n_tags = 1024, 37, 60
+    w = gpu.synth_model(seed=9, n_tags=n_tags, n_targets=90, choices=[5, 10, 2])
+    n_feat = 3 * n_tags
+    stride = gpu.lwe_row_words(n_indiv, n)
+    d_in = ctx.device_alloc(n_feat * stride * 4)
+    gpu.synth_lwe_device(ctx, 77, n, n_indiv, n_feat, d_in.ptr, stride)
+    ctx.sync()
+    rows = d_in.download(dtype=np.int32).reshape(n_feat, stride)
+    m = gpu.LweModel(ctx, w.model, n_feat, n_indiv, n)
+    L = n_indiv * (n + 1)
+    for (lo, hi, ni) in [(0, m.n_out, n_indiv), (5, 131, n_indiv), (100, 101, n_indiv), (0, m.n_out, 11)]:
+        ostride = gpu.lwe_row_words(ni, n)
+        d_out = ctx.device_alloc((hi - lo) * ostride * 4)
+        m.score_device(ni, d_in.ptr, stride, lo, hi, d_out.ptr, ostride)
+        ctx.sync()
+        got = d_out.download(dtype=np.int32).reshape(hi - lo, ostride)[:, :ni * (n + 1)]
+        sub = rows if ni == n_indiv else np.ascontiguousarray(rows[:, :ni * (n + 1)])
+        want = oracle.lwe_score(w.model.term_ptr, w.model.term_feat, w.model.term_coef, sub, ni, lo, hi, n=n)
+        np.testing.assert_array_equal(got, want)
+        d_out.free()
+    assert L == rows.shape[1] - (stride - L)
+
+
+def test_synth_lwe_matches_oracle_generator(ctx, oracle):
+    n, n_indiv, n_feat = 1024, 5, 9
+    stride = gpu.lwe_row_words(n_indiv, n)
+    d = ctx.device_alloc(n_feat * stride * 4)
+    gpu.synth_lwe_device(ctx, 1234, n, n_indiv, n_feat, d.ptr, stride)
+    ctx.sync()
+    rows = d.download(dtype=np.int32).reshape(n_feat, stride)
+    for f in (0, 4, 8):
+        want = oracle.synth_lwe_words(1234, n, n_indiv, f, 0, n_indiv * (n + 1))
+        np.testing.assert_array_equal(rows[f, :n_indiv * (n + 1)], want)
+
+
+def test_lwe_equals_sample_extract_of_trlwe(ctx, oracle):
+    """Per-individual LWE scoring of SampleExtract_i(inputs) equals
+    SampleExtract_i of the TRLWE scoring: the two layouts agree."""
+    n_tags, n_indiv = 40, 6
+    w = gpu.synth_model(seed=21, n_tags=n_tags, n_targets=30, neighbours=5)
+    rows = random_rows(8, 3 * n_tags)
+    m = gpu.TrlweModel(ctx, w.model, 3 * n_tags, n_indiv, 1, 1024)
+    trl = m.score(rows)
+    stride = gpu.lwe_row_words(n_indiv)
+    lwe_in = np.zeros((3 * n_tags, stride), np.int32)
+    for f in range(3 * n_tags):
+        for i in range(n_indiv):
+            lwe_in[f, i * 1025:(i + 1) * 1025] = oracle.sample_extract(rows[f], i)
+    lm = gpu.LweModel(ctx, w.model, 3 * n_tags, n_indiv)
+    d_in = ctx.device_alloc(lwe_in.nbytes)
+    d_in.upload(lwe_in)
+    d_out = ctx.device_alloc(lm.n_out * stride * 4)
+    lm.score_device(n_indiv, d_in.ptr, stride, 0, lm.n_out, d_out.ptr, stride)
+    ctx.sync()
+    got = d_out.download(dtype=np.int32).reshape(lm.n_out, stride)
+    for o in range(0, lm.n_out, 7):
+        for i in range(n_indiv):
+            np.testing.assert_array_equal(got[o, i * 1025:(i + 1) * 1025], oracle.sample_extract(trl[o], i))
+
+
+def test_errors_are_statuses(ctx):
+    w = gpu.synth_model(seed=1, n_tags=20, n_targets=10, neighbours=5)
+    with pytest.raises(gpu.IdashError) as e:
+        gpu.TrlweModel(ctx, w.model, 10, 1000, 1, 1024)  # features beyond 10 rows
+    assert e.value.name == "IDASH_ERR_INDEX"
+    with pytest.raises(gpu.IdashError) as e:
+        gpu.TrlweModel(ctx, w.model, 60, 1000, 2, 1024)  # 2 * 1024 > N
+    assert e.value.name == "IDASH_ERR_INVALID_ARGUMENT"
+    m = gpu.TrlweModel(ctx, w.model, 60, 1000, 1, 1024)
+    d = ctx.device_alloc(61 * 8192)
+    bad = gpu.RowLayout(8200, 0, -1, -1)  # stride not a multiple of 16
+    with pytest.raises(gpu.IdashError) as e:
+        m.score_device(d.ptr, bad, d.ptr, gpu.DENSE_TRLWE)
+    assert e.value.name == "IDASH_ERR_INVALID_ARGUMENT"
+    with pytest.raises(gpu.IdashError):
+        m.score_device(d.ptr + 4, gpu.DENSE_TRLWE, d.ptr, gpu.DENSE_TRLWE)  # misaligned payload
+    ctx.sync()
+
+
+@pytest.mark.slow
+def test_full_scale_trlwe_checksum_and_samples(ctx, oracle):
+    """80,882 targets x 3 outputs, 16,184 tags, 1,000 individuals (R = 1):
+    column sums of all outputs equal sum_f (sum_o w_of) C_f + biases (mod 2^32),
+    and sampled outputs match the oracle exactly."""
+    w = gpu.synth_model(seed=0x1DA52019, n_tags=16184, n_targets=80882, neighbours=5)
+    params = gpu.TrlweParams(1024, 1, 1000, 1, 1024, 1 << 18, 42)
+    n_rows = 3 * 16184
+    d_in = ctx.device_alloc(n_rows * 8192)
+    gpu.synth_trlwe_device(ctx, 5, params, 16184, d_in.ptr, gpu.DENSE_TRLWE)
+    m = gpu.TrlweModel(ctx, w.model, n_rows, 1000, 1, 1024)
+    d_out = ctx.device_alloc(m.n_out * 8192)
+    m.score_device(d_in.ptr, gpu.DENSE_TRLWE, d_out.ptr, gpu.DENSE_TRLWE)
+    ctx.sync()
+    rows = d_in.download(dtype=np.int32).reshape(n_rows, 2048)
+    out = d_out.download(dtype=np.int32).reshape(m.n_out, 2048)
+    colsum = out.view(np.uint32).sum(axis=0, dtype=np.uint64) & 0xFFFFFFFF
+    csr = w.model
+    wsum = np.zeros(n_rows, np.uint64)
+    bias = np.uint64(0)
+    for o in range(csr.n_out):
+        for t in range(int(csr.term_ptr[o]), int(csr.term_ptr[o + 1])):
+            f, c = int(csr.term_feat[t]), int(csr.term_coef[t]) & 0xFFFFFFFF
+            if f == 0xFFFFFFFF:
+                bias = (bias + np.uint64(c * (1 << 18))) & np.uint64(0xFFFFFFFF)
+            else:
+                wsum[f] = (wsum[f] + np.uint64(c)) & np.uint64(0xFFFFFFFF)
+    want = np.zeros(2048, np.uint64)
+    r32 = rows.view(np.uint32).astype(np.uint64)
+    for f in np.nonzero(wsum)[0]:
+        want = (want + wsum[f] * r32[f]) & np.uint64(0xFFFFFFFF)
+    want[1024:1024 + 1000] = (want[1024:1024 + 1000] + bias) & np.uint64(0xFFFFFFFF)
+    np.testing.assert_array_equal(colsum, want)
+    for lo in (0, 120003, csr.n_out - 60):
+        sub = csr.slice_outputs(lo, lo + 60)
+        got_o, _ = oracle.trlwe_score(sub.term_ptr, sub.term_feat, sub.term_coef, rows, 1000, 1, 1024)
+        np.testing.assert_array_equal(out[lo:lo + 60], got_o)
