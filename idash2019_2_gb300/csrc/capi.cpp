@@ -397,6 +397,7 @@ idash_status idash_open(idash_ctx **out, int device) {
 void idash_close(idash_ctx *ctx) {
     if (!ctx) return;
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    while (!ctx->models.empty()) idash_model_free(*ctx->models.begin());
     for (cudaEvent_t e : ctx->events) cudaEventDestroy(e);
     if (ctx->join_in) cudaEventDestroy(ctx->join_in);
     if (ctx->join_out) cudaEventDestroy(ctx->join_out);
@@ -554,6 +555,7 @@ idash_status idash_model_trlwe(idash_ctx *ctx, idash_model **model, const idash_
         idash_model_free(m);
         return s;
     }
+    ctx->models.insert(m);
     *model = m;
     return IDASH_OK;
 }
@@ -582,6 +584,7 @@ idash_status idash_model_lwe(idash_ctx *ctx, idash_model **model, const idash_lw
         idash_model_free(m);
         return s;
     }
+    ctx->models.insert(m);
     *model = m;
     return IDASH_OK;
 }
@@ -609,7 +612,10 @@ idash_status idash_model_replan(idash_model *m) {
 
 void idash_model_free(idash_model *m) {
     if (!m) return;
-    if (m->ctx && m->ctx->stream) cudaStreamSynchronize(m->ctx->stream);
+    if (m->ctx) {
+        if (m->ctx->stream) cudaStreamSynchronize(m->ctx->stream);
+        m->ctx->models.erase(m);
+    }
     m->drop_graph();
     m->free_device();
     delete m;

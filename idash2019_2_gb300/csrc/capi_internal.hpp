@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <set>
 #include <string>
 #include <vector>
 
@@ -32,6 +33,7 @@ struct idash_ctx {
 
     idash_stats stats{};
     std::string last_error;
+    std::set<idash_model *> models;  // live models; idash_close frees what is left
 
     // buffers for the host-memory path (grow only)
     uint8_t *d_in_buf = nullptr, *d_out_buf = nullptr;

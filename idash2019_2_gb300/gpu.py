@@ -7,6 +7,7 @@ output rows.  All compute goes through libidash_gpu.so; host arrays are numpy.
 from __future__ import annotations
 
 import ctypes as C
+import weakref
 from dataclasses import dataclass
 
 import numpy as np
@@ -37,9 +38,15 @@ class Context:
         if code != 0:
             raise IdashError(code, (self.lib.idash_last_error(None) or b"").decode())
         self.h = h
+        self._owned = weakref.WeakSet()  # models and buffers to release before the context
+
+    def _own(self, obj):
+        self._owned.add(obj)
 
     def close(self):
         if self.h:
+            for obj in list(self._owned):
+                obj.free()
             self.lib.idash_close(self.h)
             self.h = None
 
@@ -92,6 +99,7 @@ class DeviceBuffer:
         p = C.c_void_p()
         ctx.check(ctx.lib.idash_device_alloc(ctx.h, self.nbytes, C.byref(p)))
         self.ptr = p.value
+        ctx._own(self)
 
     def free(self):
         if self.ptr and self.ctx.h:
@@ -129,6 +137,7 @@ class HostBuffer:
         p = C.c_void_p()
         ctx.check(ctx.lib.idash_host_alloc(ctx.h, self.nbytes, C.byref(p)))
         self.ptr = p.value
+        ctx._own(self)
         self.array = np.ctypeslib.as_array((C.c_uint8 * self.nbytes).from_address(self.ptr))
 
     def free(self):
@@ -222,11 +231,12 @@ class TrlweModel:
         self.h = h
         self.n_out = csr.n_out
         self.n_in_rows = n_in_rows
+        ctx._own(self)
 
     def free(self):
-        if self.h:
+        if self.h and self.ctx.h:
             self.ctx.lib.idash_model_free(self.h)
-            self.h = None
+        self.h = None
 
     def __del__(self):
         try:
@@ -279,11 +289,12 @@ class LweModel:
                                           _p(self._keep[2], C.c_int32), n_feat_rows))
         self.h = h
         self.n_out = csr.n_out
+        ctx._own(self)
 
     def free(self):
-        if self.h:
+        if self.h and self.ctx.h:
             self.ctx.lib.idash_model_free(self.h)
-            self.h = None
+        self.h = None
 
     def __del__(self):
         try:

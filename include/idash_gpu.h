@@ -56,6 +56,8 @@ int idash_abi_version(void);
 /* Opens `device` and creates the context's stream.  Replaces nothing in the
  * reference (its only "context" is the OpenMP team, eval/idash.cpp:779). */
 idash_status idash_open(idash_ctx **ctx, int device);
+/* Waits for the context's work, frees every model still open on it, then the
+ * context.  Models of a closed context must not be used or freed again. */
 void idash_close(idash_ctx *ctx);
 /* Human-readable detail of the last failure on this context ("" if none);
  * with ctx == NULL, why the last idash_open on this thread failed. */

@@ -97,7 +97,7 @@ def test_trlwe_synth_vs_oracle(ctx, oracle, regions, kernel):
 def test_trlwe_device_path_tiles(ctx, oracle, slice_words, graph):
     """Every slice width of the window kernel, with and without graph replay,
     on the device-resident path (dense rows)."""
-    w = gpu.synth_model(seed=3, n_tags=200, n_targets=700, choices=[5, 10, 20, 30, 50])
+    w = gpu.synth_model(seed=3, n_tags=200, n_targets=700, choices=[5, 2, 3, 1])
     n_rows = 600
     rows = random_rows(5, n_rows)
     ctx.set_option("slice_words", slice_words)
@@ -120,6 +120,23 @@ def test_trlwe_device_path_tiles(ctx, oracle, slice_words, graph):
     finally:
         ctx.set_option("slice_words", 0)
         ctx.set_option("graph", 1)
+
+
+def test_large_neighbourhoods_fall_back_to_direct_kernel(ctx, oracle):
+    """50-neighbour outputs (150 window slots) do not fit a 2048-word slice
+    window; the model is planned for the direct kernel and stays exact."""
+    w = gpu.synth_model(seed=31, n_tags=200, n_targets=300, choices=[5, 50])
+    rows = random_rows(9, 600)
+    ctx.set_option("slice_words", 2048)
+    try:
+        m = gpu.TrlweModel(ctx, w.model, 600, 1000, 1, 1024)
+        assert m.info()["kernel"] == 1
+        got = m.score(rows)
+        m.free()
+    finally:
+        ctx.set_option("slice_words", 0)
+    want, _ = oracle.trlwe_score(w.model.term_ptr, w.model.term_feat, w.model.term_coef, rows, 1000, 1, 1024)
+    np.testing.assert_array_equal(got, want)
 
 
 def test_trlwe_autotune_picks_a_correct_plan(ctx, oracle):
