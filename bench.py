@@ -122,7 +122,7 @@ def dist_env():
     return rank, world, local
 
 
-def cpu_baseline(model_csr, rows, spec, min_seconds=8.0, max_reps=20):
+def cpu_baseline(model_csr, rows, spec, min_seconds=10.0, max_reps=1000):
     """The oracle's restatement of the reference loop (OpenMP over outputs,
     eval/idash.cpp:779-842) on all host cores, full workload per rep."""
     import pyoracle
@@ -182,6 +182,87 @@ def run_reference(args):
                                        f"built on this host)"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def time_on_stream(ctx, fn, steps):
+    """ms per call of fn(), CUDA events on the context's stream."""
+    import torch
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ctx.sync()
+    e0.record(stream)
+    for _ in range(steps):
+        fn()
+    e1.record(stream)
+    e1.synchronize()
+    ctx.sync()
+    return e0.elapsed_time(e1) / steps
+
+
+def section_plain(ctx, w, spec, d_in, d_out, steps):
+    """The plain per-output kernel (k_score_direct) on the same workload."""
+    from idash2019_2_gb300 import gpu
+    ctx.set_option("kernel", 1)
+    try:
+        m = gpu.TrlweModel(ctx, w.model, spec["n_rows"], spec["num_samples"], spec["regions"], spec["region_size"])
+        lay = gpu.DENSE_TRLWE
+        for _ in range(3):
+            m.score_device(d_in.ptr, lay, d_out.ptr, lay)
+        ms = time_on_stream(ctx, lambda: m.score_device(d_in.ptr, lay, d_out.ptr, lay), steps)
+        m.free()
+    finally:
+        ctx.set_option("kernel", 0)
+    preds = spec["n_indiv"] * spec["n_targets"] * 3
+    return {"value": preds / (ms / 1e3), "unit": UNIT, "ms_per_step": ms,
+            "kernel": "direct: one output per team, every input read from global memory"}
+
+
+def section_lwe(ctx, name, seed, n_indiv, n_tags, n_targets, neighbours=5, choices=None, passes=2, chunk=2048):
+    """Per-individual LWE form: inputs resident (n_indiv LWE samples of n=1024
+    per feature row), outputs produced range by range into a 2-slot HBM ring
+    (the full output does not fit in HBM)."""
+    from idash2019_2_gb300 import gpu
+    w = gpu.synth_model(seed, n_tags, n_targets, neighbours=neighbours, choices=choices)
+    n_feat = 3 * n_tags
+    stride = gpu.lwe_row_words(n_indiv)
+    L = n_indiv * 1025
+    d_in = ctx.device_alloc(n_feat * stride * 4)
+    gpu.synth_lwe_device(ctx, seed, 1024, n_indiv, n_feat, d_in.ptr, stride)
+    m = gpu.LweModel(ctx, w.model, n_feat, n_indiv)
+    ring = [ctx.device_alloc(chunk * stride * 4) for _ in range(2)]
+    ranges = [(lo, min(lo + chunk, m.n_out)) for lo in range(0, m.n_out, chunk)]
+
+    def one_pass():
+        for c, (lo, hi) in enumerate(ranges):
+            m.score_device(n_indiv, d_in.ptr, stride, lo, hi, ring[c % 2].ptr, stride)
+
+    t0 = time.perf_counter()
+    one_pass()  # first call autotunes the slice width
+    ctx.sync()
+    first_s = time.perf_counter() - t0
+    launches0 = ctx.stats()["kernel_launches"]
+    ms = time_on_stream(ctx, one_pass, passes)
+    launches = (ctx.stats()["kernel_launches"] - launches0) // passes
+    info = m.info()
+    preds = n_indiv * n_targets * 3
+    alg = info["algorithmic_in_rows"] * L * 4 + m.n_out * L * 4 + info["n_terms"] * 8 + m.n_out * 8
+    peak, _ = peaks()
+    macs = float(sum(int(w.model.term_ptr[o + 1] - w.model.term_ptr[o]) - 1 for o in range(0, m.n_out, 97))) * 97
+    out = {"value": preds / (ms / 1e3), "unit": UNIT, "ms_per_step": ms, "workload": name,
+           "individuals": n_indiv, "targets": n_targets, "tags": n_tags,
+           "neighbours": neighbours if not choices else f"uniform from {choices}",
+           "input_bytes": n_feat * stride * 4, "output_bytes_per_step": m.n_out * L * 4,
+           "kernel": "window (batched, persistent)" if info["kernel"] == 0 else "direct",
+           "slice_words": info["slice_words"], "launches_per_step": launches,
+           "first_pass_s_including_autotune": first_s,
+           "roofline": {"bound": "hbm", "achieved": alg / (ms / 1e3) / 1e9, "peak": peak, "unit": "GB/s",
+                        "frac": alg / (ms / 1e3) / 1e9 / peak, "algorithmic_bytes_per_step": alg},
+           "int_macs_per_step_est": macs * L, "imad_tops_at_this_rate": macs * L / (ms / 1e3) / 1e12}
+    for b in ring:
+        b.free()
+    d_in.free()
+    m.free()
+    return out
 
 
 def run_ours(args):
@@ -275,6 +356,26 @@ def run_ours(args):
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         rows = np.frombuffer(h_in.array, dtype=np.int32).reshape(spec["n_rows"], 2048)
         base = cpu_baseline(w.model, rows, spec)
+    h_in.free()
+    h_out.free()
+
+    forms = {}
+    sections = set(args.sections.split(",")) if args.sections else set()
+    if world == 1 and "plain" in sections:
+        forms["plain"] = section_plain(ctx, w, spec, d_in, d_out, min(args.steps, 200))
+        forms["plain"]["batched_over_plain"] = value / forms["plain"]["value"]
+    d_in.free()
+    d_out.free()
+    model.free()
+    if world == 1 and "lwe_full" in sections:
+        forms["lwe_full"] = section_lwe(ctx, "full scale, per-individual LWE: 1,000 individuals x 80,882 targets "
+                                             "x 3, 16,184 tags, 5 neighbours, n=1024", args.seed, 1000, 16184, 80882,
+                                        neighbours=5)
+    if world == 1 and "batched_uneven" in sections:
+        forms["batched_uneven"] = section_lwe(ctx, "batched uneven neighbourhoods, per-individual LWE: 1,000 "
+                                                   "individuals x 80,882 targets x 3, neighbours uniform from "
+                                                   "{5,10,20,30,50}", args.seed + 1, 1000, 16184, 80882,
+                                              choices=[5, 10, 20, 30, 50], passes=1)
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -289,8 +390,9 @@ def run_ours(args):
                              "frac": achieved / peak, "traffic": traffic, "peak_source": peak_src,
                              "algorithmic_bytes_per_launch": alg_bytes},
                 "cpu_baseline": base, "e2e": e2e, "gpu_launches": launches, "clocks": clocks}
+        if forms:
+            line["forms"] = forms
         print(json.dumps(line), flush=True)
-    model.free()
     ctx.close()
     if world > 1:
         torch.distributed.destroy_process_group()
@@ -305,6 +407,8 @@ def main():
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="trlwe_full")
     ap.add_argument("--seed", type=int, default=0x1DA52019)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--sections", default="plain,lwe_full,batched_uneven",
+                    help="extra forms measured after the headline (comma list, '' for none)")
     args = ap.parse_args()
     args.steps_given = args.steps is not None
     if args.steps is None:

@@ -179,7 +179,19 @@ std::string build_plan(const PlanInput &in, const PlanLimits &lim, Plan *plan, b
             terms += uint32_t(g.keys.size());
             ++gend;
         }
-        b.n_slots = uint32_t(win.size());
+        if (win.size() > 0xFFFFu) return "a block window needs more than 65535 slots";
+        // unrotated slots first (bulk-copied by the kernel), rotated ones after
+        // (gathered with the negacyclic sign); both parts stay sorted
+        const size_t n_unrot = size_t(std::count_if(win.begin(), win.end(),
+                                                    [](uint64_t k) { return (k & 0xFFFFFFFFu) == 0; }));
+        std::stable_partition(win.begin(), win.end(), [](uint64_t k) { return (k & 0xFFFFFFFFu) == 0; });
+        auto local_of = [&](uint64_t key) -> uint32_t {
+            const auto lo = (key & 0xFFFFFFFFu) == 0 ? win.begin() : win.begin() + n_unrot;
+            const auto hi = (key & 0xFFFFFFFFu) == 0 ? win.begin() + n_unrot : win.end();
+            return uint32_t(std::lower_bound(lo, hi, key) - win.begin());
+        };
+        b.n_slots = uint16_t(win.size());
+        b.n_rot = uint16_t(win.size() - n_unrot);
         uint32_t max_row = 0;
         for (uint64_t k : win) {
             plan->slots.push_back(PlanSlot{uint32_t(k >> 32), uint32_t(k & 0xFFFFFFFFu)});
@@ -197,15 +209,14 @@ std::string build_plan(const PlanInput &in, const PlanLimits &lim, Plan *plan, b
                 pg.out[m] = m < g.n ? uint32_t(g.o0 + m) : kNoOutput;
                 pg.bias[m] = m < g.n ? int32_t(bias[g.o0 + m]) : 0;
             }
-            for (size_t t = 0; t < g.keys.size(); ++t) {
-                const uint32_t local = uint32_t(std::lower_bound(win.begin(), win.end(), g.keys[t]) - win.begin());
-                plan->terms.push_back(PlanTerm{int32_t(g.c[0][t]), int32_t(g.c[1][t]), int32_t(g.c[2][t]), local});
-            }
+            for (size_t t = 0; t < g.keys.size(); ++t)
+                plan->terms.push_back(
+                    PlanTerm{int32_t(g.c[0][t]), int32_t(g.c[1][t]), int32_t(g.c[2][t]), local_of(g.keys[t])});
             plan->groups.push_back(pg);
         }
         b.n_groups = uint32_t(gend - gi);
         b.n_terms = uint32_t(plan->terms.size()) - b.term_begin;
-        plan->max_block_slots = std::max(plan->max_block_slots, b.n_slots);
+        plan->max_block_slots = std::max<uint32_t>(plan->max_block_slots, b.n_slots);
         plan->max_block_terms = std::max(plan->max_block_terms, b.n_terms);
         plan->max_block_groups = std::max(plan->max_block_groups, b.n_groups);
         plan->blocks.push_back(b);

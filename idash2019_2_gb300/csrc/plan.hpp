@@ -21,11 +21,14 @@
 namespace idash {
 
 struct PlanBlock {
-    uint32_t slot_begin, n_slots;
+    uint32_t slot_begin;
+    uint16_t n_slots;   // unrotated slots first, then n_rot rotated ones
+    uint16_t n_rot;
     uint32_t group_begin, n_groups;
     uint32_t term_begin, n_terms;
     uint32_t out_lo, out_hi;  // outputs covered: [out_lo, out_hi)
 };
+static_assert(sizeof(PlanBlock) == 32, "PlanBlock layout");
 
 struct PlanSlot {
     uint32_t row;  // input row

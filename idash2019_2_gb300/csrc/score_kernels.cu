@@ -11,9 +11,13 @@
 // k_score_window  (batched): persistent CTAs pull (block, slice) tiles from an
 //   atomic counter; each tile's input window is staged into shared memory with
 //   cp.async.bulk (completed on an mbarrier, waits bounded), then every thread
-//   accumulates 8 columns x G outputs with 16-byte shared-memory loads.
+//   accumulates Q quads of columns x G outputs from 16-byte shared loads.
 // k_score_direct  (plain): one CTA per tile, each output read straight from
 //   global memory term by term - the reference's per-output loop on the GPU.
+//
+// A thread owns Q quads (4 consecutive columns each); quad k of the thread at
+// lane l of its team sits at column 4*l + 4*k*TEAM of the slice, so a warp's
+// 16-byte loads and stores of one quad are contiguous.
 #include "common.cuh"
 #include "score_kernels.cuh"
 
@@ -32,25 +36,29 @@ __device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
 }
 
-// Epilogue masks for the 8 columns a thread owns (bits 0-3: q0..q0+3,
-// bits 4-7: q1..q1+3): which columns receive the bias, which are zeroed.
-__device__ __forceinline__ void column_masks(const ScoreArgs &a, uint32_t c0, uint32_t q0, uint32_t q1,
-                                             uint32_t &bias_mask, uint32_t &zero_mask) {
+// Epilogue masks over the thread's 4Q columns (bit 4k+e: quad k, element e):
+// which columns receive the bias, which are zeroed.
+template <int Q, int TEAM>
+__device__ __forceinline__ void column_masks(const ScoreArgs &a, uint32_t c0, uint32_t lane, uint32_t &bias_mask,
+                                             uint32_t &zero_mask) {
     bias_mask = 0;
     zero_mask = 0;
 #pragma unroll
-    for (int e = 0; e < 8; ++e) {
-        const uint32_t c = c0 + (e < 4 ? q0 + e : q1 + (e - 4));
-        if (a.form == kFormTrlwe) {
-            if (c >= a.N) {
-                const uint32_t j = c - a.N;
-                if (j < a.num_samples) bias_mask |= 1u << e;
-                if (j >= a.region_size) zero_mask |= 1u << e;
+    for (int k = 0; k < Q; ++k)
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            const uint32_t c = c0 + 4 * lane + 4 * k * TEAM + e;
+            const uint32_t bit = 1u << (4 * k + e);
+            if (a.form == kFormTrlwe) {
+                if (c >= a.N) {
+                    const uint32_t j = c - a.N;
+                    if (j < a.num_samples) bias_mask |= bit;
+                    if (j >= a.region_size) zero_mask |= bit;
+                }
+            } else if (c % a.lwe_n1 == a.lwe_n1 - 1) {
+                bias_mask |= bit;
             }
-        } else {
-            if (c % a.lwe_n1 == a.lwe_n1 - 1) bias_mask |= 1u << e;
         }
-    }
 }
 
 __device__ __forceinline__ void store_quad(uint8_t *row, uint32_t q, uint32_t valid, uint4 v) {
@@ -65,44 +73,59 @@ __device__ __forceinline__ void store_quad(uint8_t *row, uint32_t q, uint32_t va
     }
 }
 
-template <int G>
-__device__ __forceinline__ void write_outputs(const ScoreArgs &a, const PlanGroup &gr, const uint32_t (&acc)[G][8],
-                                              uint32_t c0, uint32_t q0, uint32_t q1, uint32_t valid,
-                                              uint32_t bias_mask, uint32_t zero_mask) {
+// Accumulators start at the bias on the columns that take it (the bias of
+// eval/idash.cpp:805-810 folded in before the terms; addition commutes).
+template <int G, int Q>
+__device__ __forceinline__ void init_acc(uint32_t (&acc)[G][4 * Q], const PlanGroup &gr, uint32_t bias_mask) {
+#pragma unroll
+    for (int m = 0; m < G; ++m)
+#pragma unroll
+        for (int e = 0; e < 4 * Q; ++e) acc[m][e] = 0;
+    if (bias_mask) {
+#pragma unroll
+        for (int m = 0; m < G; ++m)
+#pragma unroll
+            for (int e = 0; e < 4 * Q; ++e)
+                if (bias_mask & (1u << e)) acc[m][e] = uint32_t(gr.bias[m]);
+    }
+}
+
+template <int G, int Q, int TEAM>
+__device__ __forceinline__ void write_outputs(const ScoreArgs &a, const PlanGroup &gr, uint32_t (&acc)[G][4 * Q],
+                                              uint32_t c0, uint32_t lane, uint32_t valid, uint32_t zero_mask) {
 #pragma unroll
     for (int m = 0; m < G; ++m) {
         const uint32_t o = gr.out[m];
         if (o == kNoOutput || o < a.out_lo || o >= a.out_hi) continue;
-        const uint32_t bias = uint32_t(gr.bias[m]);
-        uint32_t v[8];
+        if (zero_mask) {
 #pragma unroll
-        for (int e = 0; e < 8; ++e) {
-            uint32_t x = acc[m][e];
-            if (bias_mask & (1u << e)) x += bias;
-            if (zero_mask & (1u << e)) x = 0;
-            v[e] = x;
+            for (int e = 0; e < 4 * Q; ++e)
+                if (zero_mask & (1u << e)) acc[m][e] = 0;
         }
         const uint64_t r = a.out_row_map ? uint64_t(a.out_row_map[o]) : uint64_t(o) - a.out_row_base;
         uint8_t *row = a.out + r * a.out_stride + uint64_t(c0) * 4;
-        if (q0 < valid) store_quad(row, q0, valid, make_uint4(v[0], v[1], v[2], v[3]));
-        if (q1 < valid) store_quad(row, q1, valid, make_uint4(v[4], v[5], v[6], v[7]));
+#pragma unroll
+        for (int k = 0; k < Q; ++k) {
+            const uint32_t q = 4 * lane + 4 * k * TEAM;
+            if (q < valid)
+                store_quad(row, q, valid,
+                           make_uint4(acc[m][4 * k], acc[m][4 * k + 1], acc[m][4 * k + 2], acc[m][4 * k + 3]));
+        }
     }
 }
 
-template <int G>
-__device__ __forceinline__ void mac8(uint32_t (&acc)[G][8], const PlanTerm &tm, const uint4 &x0, const uint4 &x1) {
+template <int G, int Q>
+__device__ __forceinline__ void mac(uint32_t (&acc)[G][4 * Q], const PlanTerm &tm, const uint4 (&x)[Q]) {
     const uint32_t c[3] = {uint32_t(tm.c0), uint32_t(tm.c1), uint32_t(tm.c2)};
 #pragma unroll
-    for (int m = 0; m < G; ++m) {
-        acc[m][0] += c[m] * x0.x;
-        acc[m][1] += c[m] * x0.y;
-        acc[m][2] += c[m] * x0.z;
-        acc[m][3] += c[m] * x0.w;
-        acc[m][4] += c[m] * x1.x;
-        acc[m][5] += c[m] * x1.y;
-        acc[m][6] += c[m] * x1.z;
-        acc[m][7] += c[m] * x1.w;
-    }
+    for (int m = 0; m < G; ++m)
+#pragma unroll
+        for (int k = 0; k < Q; ++k) {
+            acc[m][4 * k + 0] += c[m] * x[k].x;
+            acc[m][4 * k + 1] += c[m] * x[k].y;
+            acc[m][4 * k + 2] += c[m] * x[k].z;
+            acc[m][4 * k + 3] += c[m] * x[k].w;
+        }
 }
 
 // Value of column c (of the 2N-word TRLWE row) of X^(-m) * row:
@@ -114,10 +137,11 @@ __device__ __forceinline__ uint32_t rotated_word(const uint32_t *src, uint32_t c
     return t < N ? src[p * N + t] : 0u - src[p * N + t - N];
 }
 
-template <int W, int G>
+template <int W, int G, int Q>
 __global__ void __launch_bounds__(kThreads) k_score_window(const ScoreArgs a) {
-    constexpr int TEAM = W / 8;
+    constexpr int TEAM = W / (4 * Q);
     constexpr int NTEAMS = kThreads / TEAM;
+    static_assert(TEAM >= 32 && kThreads % TEAM == 0, "a team is one or more whole warps");
     extern __shared__ __align__(128) uint8_t smem[];
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem);
     uint32_t *tile_s = reinterpret_cast<uint32_t *>(smem + 8);
@@ -133,7 +157,6 @@ __global__ void __launch_bounds__(kThreads) k_score_window(const ScoreArgs a) {
     __syncthreads();
 
     const uint32_t team = tid / TEAM, lane = tid % TEAM;
-    const uint32_t q0 = 4 * lane, q1 = 4 * lane + 4 * TEAM;
     uint32_t phase = 0;
 
     for (;;) {
@@ -154,9 +177,9 @@ __global__ void __launch_bounds__(kThreads) k_score_window(const ScoreArgs a) {
         if (tid < 32) {
             if (tid == 0) fence_proxy_async_smem();
             __syncwarp();
-            for (uint32_t s = tid; s < blk.n_slots; s += 32) {
+            const uint32_t n_unrot = uint32_t(blk.n_slots) - blk.n_rot;
+            for (uint32_t s = tid; s < n_unrot; s += 32) {
                 const PlanSlot sl = a.slots[blk.slot_begin + s];
-                if (sl.rot != 0) continue;
                 if (sl.row >= a.n_rows) {
                     report_error(a.err, kDevBadIndex);
                     continue;
@@ -177,12 +200,13 @@ __global__ void __launch_bounds__(kThreads) k_score_window(const ScoreArgs a) {
             if (tid == 0) mbar_arrive(bar);
         }
         // Rotated slots (TRLWE with NUM_REGIONS > 1): gathered by all threads.
-        if (a.form == kFormTrlwe) {
-            for (uint32_t s = 0; s < blk.n_slots; ++s) {
+        if (blk.n_rot) {
+            for (uint32_t s = uint32_t(blk.n_slots) - blk.n_rot; s < blk.n_slots; ++s) {
                 const PlanSlot sl = a.slots[blk.slot_begin + s];
-                if (sl.rot == 0 || sl.row >= a.n_rows) continue;
+                if (sl.row >= a.n_rows) continue;
                 const uint32_t *src = reinterpret_cast<const uint32_t *>(a.in + uint64_t(sl.row) * a.in_stride);
-                for (uint32_t x = tid; x < valid; x += kThreads) win[size_t(s) * W + x] = rotated_word(src, c0 + x, sl.rot, a.N);
+                for (uint32_t x = tid; x < valid; x += kThreads)
+                    win[size_t(s) * W + x] = rotated_word(src, c0 + x, sl.rot, a.N);
             }
         }
         __syncthreads();
@@ -196,36 +220,34 @@ __global__ void __launch_bounds__(kThreads) k_score_window(const ScoreArgs a) {
         phase ^= 1u;
 
         uint32_t bias_mask, zero_mask;
-        column_masks(a, c0, q0, q1, bias_mask, zero_mask);
+        column_masks<Q, TEAM>(a, c0, lane, bias_mask, zero_mask);
+        const uint32_t *wlane = win + 4 * lane;
         for (uint32_t g = team; g < blk.n_groups; g += NTEAMS) {
             const PlanGroup gr = groups_s[g];
-            uint32_t acc[G][8];
-#pragma unroll
-            for (int m = 0; m < G; ++m)
-#pragma unroll
-                for (int e = 0; e < 8; ++e) acc[m][e] = 0;
+            uint32_t acc[G][4 * Q];
+            init_acc<G, Q>(acc, gr, bias_mask);
             const PlanTerm *tp = terms_s + gr.term_begin;
 #pragma unroll 2
             for (uint32_t t = 0; t < gr.n_terms; ++t) {
                 const PlanTerm tm = tp[t];
-                const uint32_t *w = win + size_t(tm.slot) * W;
-                const uint4 x0 = *reinterpret_cast<const uint4 *>(w + q0);
-                const uint4 x1 = *reinterpret_cast<const uint4 *>(w + q1);
-                mac8<G>(acc, tm, x0, x1);
+                const uint32_t *w = wlane + size_t(tm.slot) * W;
+                uint4 x[Q];
+#pragma unroll
+                for (int k = 0; k < Q; ++k) x[k] = *reinterpret_cast<const uint4 *>(w + 4 * k * TEAM);
+                mac<G, Q>(acc, tm, x);
             }
-            write_outputs<G>(a, gr, acc, c0, q0, q1, valid, bias_mask, zero_mask);
+            write_outputs<G, Q, TEAM>(a, gr, acc, c0, lane, valid, zero_mask);
         }
         __syncthreads();
     }
 }
 
-template <int W, int G>
+template <int W, int G, int Q>
 __global__ void __launch_bounds__(kThreads) k_score_direct(const ScoreArgs a) {
-    constexpr int TEAM = W / 8;
+    constexpr int TEAM = W / (4 * Q);
     constexpr int NTEAMS = kThreads / TEAM;
     const uint32_t tid = threadIdx.x;
     const uint32_t team = tid / TEAM, lane = tid % TEAM;
-    const uint32_t q0 = 4 * lane, q1 = 4 * lane + 4 * TEAM;
     const uint32_t tile = blockIdx.x;
     if (tile >= a.n_tiles) return;
     const uint32_t b = a.block_lo + tile % a.n_blocks;
@@ -236,14 +258,11 @@ __global__ void __launch_bounds__(kThreads) k_score_direct(const ScoreArgs a) {
     const uint32_t vpad = (valid + 3u) & ~3u;
 
     uint32_t bias_mask, zero_mask;
-    column_masks(a, c0, q0, q1, bias_mask, zero_mask);
+    column_masks<Q, TEAM>(a, c0, lane, bias_mask, zero_mask);
     for (uint32_t g = team; g < blk.n_groups; g += NTEAMS) {
         const PlanGroup gr = a.groups[blk.group_begin + g];
-        uint32_t acc[G][8];
-#pragma unroll
-        for (int m = 0; m < G; ++m)
-#pragma unroll
-            for (int e = 0; e < 8; ++e) acc[m][e] = 0;
+        uint32_t acc[G][4 * Q];
+        init_acc<G, Q>(acc, gr, bias_mask);
         const PlanTerm *tp = a.terms + blk.term_begin + gr.term_begin;
         for (uint32_t t = 0; t < gr.n_terms; ++t) {
             const PlanTerm tm = tp[t];
@@ -253,30 +272,27 @@ __global__ void __launch_bounds__(kThreads) k_score_direct(const ScoreArgs a) {
                 continue;
             }
             const uint8_t *src = a.in + uint64_t(sl.row) * a.in_stride;
-            uint4 x0 = make_uint4(0, 0, 0, 0), x1 = make_uint4(0, 0, 0, 0);
-            if (sl.rot == 0) {
-                if (q0 < vpad) {
-                    const int4 v = ldg_nc_v4(src + (uint64_t(c0) + q0) * 4);
-                    x0 = make_uint4(uint32_t(v.x), uint32_t(v.y), uint32_t(v.z), uint32_t(v.w));
-                }
-                if (q1 < vpad) {
-                    const int4 v = ldg_nc_v4(src + (uint64_t(c0) + q1) * 4);
-                    x1 = make_uint4(uint32_t(v.x), uint32_t(v.y), uint32_t(v.z), uint32_t(v.w));
-                }
-            } else {
-                const uint32_t *s32 = reinterpret_cast<const uint32_t *>(src);
-                uint32_t tmp[8];
+            uint4 x[Q];
 #pragma unroll
-                for (int e = 0; e < 8; ++e) {
-                    const uint32_t q = e < 4 ? q0 + e : q1 + (e - 4);
-                    tmp[e] = q < valid ? rotated_word(s32, c0 + q, sl.rot, a.N) : 0u;
+            for (int k = 0; k < Q; ++k) {
+                const uint32_t q = 4 * lane + 4 * k * TEAM;
+                x[k] = make_uint4(0, 0, 0, 0);
+                if (sl.rot == 0) {
+                    if (q < vpad) {
+                        const int4 v = ldg_nc_v4(src + (uint64_t(c0) + q) * 4);
+                        x[k] = make_uint4(uint32_t(v.x), uint32_t(v.y), uint32_t(v.z), uint32_t(v.w));
+                    }
+                } else {
+                    const uint32_t *s32 = reinterpret_cast<const uint32_t *>(src);
+                    x[k].x = q + 0 < valid ? rotated_word(s32, c0 + q + 0, sl.rot, a.N) : 0u;
+                    x[k].y = q + 1 < valid ? rotated_word(s32, c0 + q + 1, sl.rot, a.N) : 0u;
+                    x[k].z = q + 2 < valid ? rotated_word(s32, c0 + q + 2, sl.rot, a.N) : 0u;
+                    x[k].w = q + 3 < valid ? rotated_word(s32, c0 + q + 3, sl.rot, a.N) : 0u;
                 }
-                x0 = make_uint4(tmp[0], tmp[1], tmp[2], tmp[3]);
-                x1 = make_uint4(tmp[4], tmp[5], tmp[6], tmp[7]);
             }
-            mac8<G>(acc, tm, x0, x1);
+            mac<G, Q>(acc, tm, x);
         }
-        write_outputs<G>(a, gr, acc, c0, q0, q1, valid, bias_mask, zero_mask);
+        write_outputs<G, Q, TEAM>(a, gr, acc, c0, lane, valid, zero_mask);
     }
 }
 
@@ -306,14 +322,16 @@ __global__ void k_finalize(const FinalizeArgs a) {
 
 using KernelFn = void (*)(const ScoreArgs);
 
+// Columns per thread: 16 (4 quads) from 512-word slices up, 8 below; the
+// direct kernel keeps 8 so that each output has 256 threads of loads in flight.
 template <int G>
 KernelFn pick(KernelKind kind, uint32_t w) {
     const bool win = kind == KernelKind::kWindow;
     switch (w) {
-        case 256: return win ? k_score_window<256, G> : k_score_direct<256, G>;
-        case 512: return win ? k_score_window<512, G> : k_score_direct<512, G>;
-        case 1024: return win ? k_score_window<1024, G> : k_score_direct<1024, G>;
-        case 2048: return win ? k_score_window<2048, G> : k_score_direct<2048, G>;
+        case 256: return win ? k_score_window<256, G, 2> : k_score_direct<256, G, 2>;
+        case 512: return win ? k_score_window<512, G, 4> : k_score_direct<512, G, 2>;
+        case 1024: return win ? k_score_window<1024, G, 4> : k_score_direct<1024, G, 2>;
+        case 2048: return win ? k_score_window<2048, G, 4> : k_score_direct<2048, G, 2>;
         default: return nullptr;
     }
 }
