@@ -30,6 +30,7 @@ NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O3"
 LIB_SOURCES = [
     "csrc/score_kernels.cu",
     "csrc/synth.cu",
+    "csrc/noalloc.cu",
     "csrc/capi.cpp",
     "csrc/plan.cpp",
     "csrc/host/idash_host.cpp",

@@ -301,6 +301,8 @@ bool autotune_wanted(const idash_model *m) {
 
 }  // namespace
 
+void idash_set_thread_error(const std::string &msg) { g_open_error = msg; }
+
 cudaEvent_t idash_ctx::event(size_t i) {
     while (events.size() <= i) {
         cudaEvent_t e = nullptr;

@@ -12,6 +12,10 @@
 #include "plan.hpp"
 #include "score_kernels.cuh"
 
+// Message returned by idash_last_error(NULL) on this thread (entry points
+// that have no context: idash_open failures, idash_score_trlwe_noalloc).
+void idash_set_thread_error(const std::string &msg);
+
 struct idash_ctx {
     int device = 0;
     int sm_count = 0;

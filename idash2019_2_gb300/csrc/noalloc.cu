@@ -1,0 +1,247 @@
+// idash_score_trlwe_noalloc: TRLWE scoring that allocates no device or
+// page-locked memory.
+//
+// Some callers cannot call cudaMalloc.  Examples: a service whose framework
+// reserves the GPU's memory for its own pool up front, a process capped by a
+// per-client device-memory limit that it has already reached, or a
+// latency-bound loop that cannot afford the implicit synchronisation of
+// cudaMalloc/cudaFree.  They still own the input and output buffers.  This
+// entry point needs nothing else from the device heap.  Its scratch is the
+// array below: the planned work list (blocks, slots, groups, terms), the
+// window kernel's tile counter, the device error word and the variance
+// program.  The array is a fixed part of the library's device image, so every
+// GPU that loads the library holds it until the process exits.
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "capi_internal.hpp"
+
+namespace {
+
+// 32 MiB per device: enough for the full-scale model (242,646 outputs,
+// 5 neighbours) with room to spare.  Larger models are refused.
+constexpr size_t kScratchBytes = size_t(32) << 20;
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_setup_mutex;
+unsigned char *g_scratch_addr[kMaxDevices] = {};  // device address per device, set on first call
+
+size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+idash_status fail(idash_status s, const std::string &msg) {
+    idash_set_thread_error(msg);
+    return s;
+}
+
+// First call on a device: resolve the array's device address with that
+// device current, and allow the window kernels their shared memory.
+idash_status setup_device(int dev, unsigned char **addr, int *sm_count, size_t *smem_optin) {
+    cudaDeviceProp prop{};
+    cudaError_t e = cudaGetDeviceProperties(&prop, dev);
+    if (e != cudaSuccess) return fail(IDASH_ERR_CUDA, std::string("cudaGetDeviceProperties: ") + cudaGetErrorString(e));
+    *sm_count = prop.multiProcessorCount;
+    *smem_optin = prop.sharedMemPerBlockOptin;
+    std::lock_guard<std::mutex> lock(g_setup_mutex);
+    if (!g_scratch_addr[dev]) {
+        void *p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess)
+            return fail(IDASH_ERR_CUDA, std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e));
+        e = idash::configure_window_kernels(prop.sharedMemPerBlockOptin);
+        if (e != cudaSuccess) return fail(IDASH_ERR_CUDA, std::string("configure kernels: ") + cudaGetErrorString(e));
+        g_scratch_addr[dev] = static_cast<unsigned char *>(p);
+    }
+    *addr = g_scratch_addr[dev];
+    return IDASH_OK;
+}
+
+bool layout_ok(const void *base, const idash_row_layout *l, uint64_t payload) {
+    if (!l || l->row_stride % 16 || ((reinterpret_cast<uintptr_t>(base) + l->payload_offset) & 15u)) return false;
+    if (l->payload_offset + payload > l->row_stride) return false;
+    auto clash = [&](int64_t off, uint64_t len) {
+        return off >= 0 && (uint64_t(off) + len > l->row_stride ||
+                            (uint64_t(off) < l->payload_offset + payload && uint64_t(off) + len > l->payload_offset));
+    };
+    if (clash(l->variance_offset, 8) || clash(l->header_offset, 8)) return false;
+    if (l->variance_offset >= 0 && (reinterpret_cast<uintptr_t>(base) + l->variance_offset) % 8) return false;
+    return true;
+}
+
+}  // namespace
+
+extern "C" idash_status idash_score_trlwe_noalloc(const idash_trlwe_params *p, uint64_t n_out, const uint64_t *term_ptr,
+                                                  const uint32_t *term_feat, const int32_t *term_coef,
+                                                  uint64_t n_in_rows, const void *d_in,
+                                                  const idash_row_layout *in_layout, void *d_out,
+                                                  const idash_row_layout *out_layout, void *stream) {
+    using namespace idash;
+    if (!p || !d_in || !d_out || !in_layout || !out_layout || (n_out && (!term_ptr || (term_ptr[n_out] &&
+                                                                                      (!term_feat || !term_coef)))))
+        return fail(IDASH_ERR_INVALID_ARGUMENT, "null argument");
+    if (p->k != 1 || p->N == 0 || p->N % 256 || p->N > 4096)
+        return fail(IDASH_ERR_UNSUPPORTED, "need k = 1 and N a multiple of 256 up to 4096");
+    if (p->num_regions == 0 || p->region_size == 0 || uint64_t(p->num_regions) * p->region_size > p->N ||
+        p->num_samples > p->region_size)
+        return fail(IDASH_ERR_INVALID_ARGUMENT, "need NUM_REGIONS*REGION_SIZE <= N and NUM_SAMPLES <= REGION_SIZE");
+    const uint64_t payload = uint64_t(2) * p->N * 4;
+    if (!layout_ok(d_in, in_layout, payload) || !layout_ok(d_out, out_layout, payload))
+        return fail(IDASH_ERR_INVALID_ARGUMENT, "row layout: stride, alignment or field offsets");
+    if (n_out == 0) return IDASH_OK;
+
+    int dev = 0;
+    cudaError_t ce = cudaGetDevice(&dev);
+    if (ce != cudaSuccess) return fail(IDASH_ERR_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(ce));
+    if (dev < 0 || dev >= kMaxDevices) return fail(IDASH_ERR_UNSUPPORTED, "device ordinal beyond 63");
+    unsigned char *scratch = nullptr;
+    int sm_count = 0;
+    size_t smem_optin = 0;
+    idash_status s = setup_device(dev, &scratch, &sm_count, &smem_optin);
+    if (s != IDASH_OK) return s;
+
+    // Plan on the host (ordinary heap memory): the window kernel with the
+    // widest slice whose window holds every output's slots, 2 CTAs per SM.
+    PlanInput in;
+    in.form = Form::kTrlwe;
+    in.n_out = n_out;
+    in.term_ptr = term_ptr;
+    in.term_feat = term_feat;
+    in.term_coef = term_coef;
+    in.one_t32 = p->one_t32;
+    in.N = p->N;
+    in.num_regions = p->num_regions;
+    in.region_size = p->region_size;
+    in.n_rows = n_in_rows;
+    Plan plan;
+    KernelKind kind = KernelKind::kDirect;
+    uint32_t w = 512, g = 1;
+    std::string err;
+    bool index_error = false;
+    for (uint32_t cand : {1024u, 512u, 256u}) {
+        const size_t budget = std::min<size_t>(233472 / 2 - 1024, smem_optin);
+        PlanLimits lim;
+        lim.group_size = 3;
+        lim.max_groups = 64;
+        lim.max_terms = uint32_t((budget - 128 - 64 * sizeof(PlanGroup)) / 4 / sizeof(PlanTerm));
+        lim.max_slots = uint32_t((budget - 128 - 64 * sizeof(PlanGroup) - lim.max_terms * sizeof(PlanTerm)) /
+                                 (size_t(cand) * 4));
+        err = build_plan(in, lim, &plan, &index_error);
+        if (err.empty()) {
+            kind = KernelKind::kWindow;
+            w = cand;
+            g = 3;
+            break;
+        }
+        if (index_error) return fail(IDASH_ERR_INDEX, err);
+    }
+    if (kind == KernelKind::kDirect) {
+        PlanLimits lim;
+        lim.group_size = 1;
+        lim.max_slots = lim.max_terms = 0xFFFFFFFFu;
+        lim.max_groups = 8;
+        err = build_plan(in, lim, &plan, &index_error);
+        if (!err.empty()) return fail(index_error ? IDASH_ERR_INDEX : IDASH_ERR_UNSUPPORTED, err);
+    }
+
+    // Carve the scratch: error word + tile counter, then the tables.
+    const bool want_var = out_layout->variance_offset >= 0;
+    size_t off = 256;
+    auto take = [&](size_t bytes) {
+        const size_t at = off;
+        off = align256(off + std::max<size_t>(bytes, 1));
+        return at;
+    };
+    const size_t o_blocks = take(plan.blocks.size() * sizeof(PlanBlock));
+    const size_t o_slots = take(plan.slots.size() * sizeof(PlanSlot));
+    const size_t o_groups = take(plan.groups.size() * sizeof(PlanGroup));
+    const size_t o_terms = take(plan.terms.size() * sizeof(PlanTerm));
+    const size_t o_vptr = want_var ? take(plan.var_ptr.size() * 8) : 0;
+    const size_t o_vrow = want_var ? take(plan.var_row.size() * 4) : 0;
+    const size_t o_vcoef = want_var ? take(plan.var_coef.size() * 4) : 0;
+    if (off > kScratchBytes)
+        return fail(IDASH_ERR_INVALID_ARGUMENT, "model needs " + std::to_string(off >> 20) +
+                                                    " MiB of scratch; the no-allocation entry point holds 32 MiB");
+
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    auto put = [&](size_t at, const void *src, size_t bytes) -> cudaError_t {
+        return bytes ? cudaMemcpyAsync(scratch + at, src, bytes, cudaMemcpyHostToDevice, st) : cudaSuccess;
+    };
+    ce = cudaMemsetAsync(scratch, 0, 256, st);  // error word and tile counter start at zero
+    if (ce == cudaSuccess) ce = put(o_blocks, plan.blocks.data(), plan.blocks.size() * sizeof(PlanBlock));
+    if (ce == cudaSuccess) ce = put(o_slots, plan.slots.data(), plan.slots.size() * sizeof(PlanSlot));
+    if (ce == cudaSuccess) ce = put(o_groups, plan.groups.data(), plan.groups.size() * sizeof(PlanGroup));
+    if (ce == cudaSuccess) ce = put(o_terms, plan.terms.data(), plan.terms.size() * sizeof(PlanTerm));
+    if (ce == cudaSuccess && want_var) {
+        ce = put(o_vptr, plan.var_ptr.data(), plan.var_ptr.size() * 8);
+        if (ce == cudaSuccess) ce = put(o_vrow, plan.var_row.data(), plan.var_row.size() * 4);
+        if (ce == cudaSuccess) ce = put(o_vcoef, plan.var_coef.data(), plan.var_coef.size() * 4);
+    }
+    if (ce != cudaSuccess) return fail(IDASH_ERR_CUDA, std::string("scratch upload: ") + cudaGetErrorString(ce));
+
+    uint32_t *d_err = reinterpret_cast<uint32_t *>(scratch);
+    ScoreArgs a{};
+    a.blocks = reinterpret_cast<const PlanBlock *>(scratch + o_blocks);
+    a.slots = reinterpret_cast<const PlanSlot *>(scratch + o_slots);
+    a.groups = reinterpret_cast<const PlanGroup *>(scratch + o_groups);
+    a.terms = reinterpret_cast<const PlanTerm *>(scratch + o_terms);
+    a.block_lo = 0;
+    a.n_blocks = uint32_t(plan.blocks.size());
+    a.row_words = 2 * p->N;
+    a.n_slices = (a.row_words + w - 1) / w;
+    a.n_tiles = a.n_blocks * a.n_slices;
+    a.n_rows = uint32_t(std::min<uint64_t>(n_in_rows, 0xFFFFFFFFull));
+    a.in = static_cast<const uint8_t *>(d_in) + in_layout->payload_offset;
+    a.in_stride = in_layout->row_stride;
+    a.out = static_cast<uint8_t *>(d_out) + out_layout->payload_offset;
+    a.out_stride = out_layout->row_stride;
+    a.out_lo = 0;
+    a.out_hi = n_out;
+    a.out_row_base = 0;
+    a.out_row_map = nullptr;
+    a.form = kFormTrlwe;
+    a.N = p->N;
+    a.num_samples = p->num_samples;
+    a.region_size = p->region_size;
+    a.max_slots = plan.max_block_slots;
+    a.max_terms = plan.max_block_terms;
+    a.max_groups = plan.max_block_groups;
+    a.tile_counter = reinterpret_cast<uint32_t *>(scratch + 4);
+    a.err = d_err;
+    uint32_t ctas = 0;
+    if (kind == KernelKind::kWindow) {
+        const int occ = window_ctas_per_sm(w, g, window_smem_bytes(w, a.max_slots, a.max_terms, a.max_groups));
+        if (occ <= 0) return fail(IDASH_ERR_CUDA, "window kernel cannot be resident");
+        ctas = uint32_t(sm_count) * uint32_t(std::min(occ, 2));
+    }
+    ce = launch_score(kind, w, g, a, ctas, st);
+    if (ce == cudaSuccess && (out_layout->variance_offset >= 0 || out_layout->header_offset >= 0)) {
+        FinalizeArgs f{};
+        f.var_ptr = reinterpret_cast<const uint64_t *>(scratch + o_vptr);
+        f.var_row = reinterpret_cast<const uint32_t *>(scratch + o_vrow);
+        f.var_coef = reinterpret_cast<const int32_t *>(scratch + o_vcoef);
+        f.out_index = nullptr;
+        f.out_row_map = nullptr;
+        f.o_begin = 0;
+        f.o_end = n_out;
+        f.in_rows = static_cast<const uint8_t *>(d_in);
+        f.in_stride = in_layout->row_stride;
+        f.in_var_off = want_var ? in_layout->variance_offset : -1;
+        f.out_rows = static_cast<uint8_t *>(d_out);
+        f.out_stride = out_layout->row_stride;
+        f.out_var_off = out_layout->variance_offset;
+        f.out_hdr_off = out_layout->header_offset;
+        f.tag = p->record_tag;
+        ce = launch_finalize(f, st);
+    }
+    if (ce != cudaSuccess) return fail(IDASH_ERR_CUDA, std::string("launch: ") + cudaGetErrorString(ce));
+    // Return only once the outputs are written, with the kernels' verdict.
+    ce = cudaStreamSynchronize(st);
+    uint32_t word = 0;
+    if (ce == cudaSuccess) ce = cudaMemcpy(&word, d_err, sizeof(word), cudaMemcpyDeviceToHost);
+    if (ce != cudaSuccess) return fail(IDASH_ERR_CUDA, std::string("sync: ") + cudaGetErrorString(ce));
+    if (word == kDevTimeout) return fail(IDASH_ERR_DEVICE_TIMEOUT, "a device-side wait expired");
+    if (word != kDevOk) return fail(IDASH_ERR_INDEX, "a kernel met an input row outside its buffer");
+    return IDASH_OK;
+}

@@ -182,6 +182,30 @@ idash_status idash_model_get_info(const idash_model *model, idash_model_info *in
 idash_status idash_model_replan(idash_model *model);
 void idash_model_free(idash_model *model);
 
+/* ------------------------------------------- scoring without allocation
+ * No counterpart in the reference.  For callers that cannot call cudaMalloc:
+ * a service whose framework reserves the GPU's memory for its own pool, a
+ * process at its per-client device-memory limit, or a latency-bound loop
+ * that cannot take the implicit synchronisation of cudaMalloc/cudaFree.  The
+ * caller passes the model (host CSR, as idash_model_trlwe) and device input
+ * and output rows, as idash_score_trlwe_device (output o -> row o); nothing
+ * else comes from the device heap.  The plan, tile counter, error word and
+ * variance program live in a fixed 32 MiB array that every GPU loading the
+ * library holds until the process exits; a model whose plan does not fit is
+ * refused with IDASH_ERR_INVALID_ARGUMENT before anything is launched.
+ * Runs on the calling thread's current device, on `stream` (NULL: the legacy
+ * default stream), and returns after the outputs are written.  The first call
+ * on a device resolves the array's address with that device current; make
+ * that first call before any stream capture.  Every call reuses the same
+ * array (it keeps the last call's contents; what must start at zero is
+ * cleared by each call): calls that overlap on one GPU, from several threads
+ * or streams, race and must be serialised by the caller.  Host-side planning
+ * uses ordinary heap memory; no device or page-locked memory is allocated. */
+idash_status idash_score_trlwe_noalloc(const idash_trlwe_params *params, uint64_t n_out, const uint64_t *term_ptr,
+                                       const uint32_t *term_feat, const int32_t *term_coef, uint64_t n_in_rows,
+                                       const void *d_in, const idash_row_layout *in_layout, void *d_out,
+                                       const idash_row_layout *out_layout, void *stream);
+
 /* ------------------------------------------- the cloud step on files
  * eval/cloud.cpp:3-28 as one call: reads params.bin (eval/idash.cpp:200-261),
  * the model directory of <pos>_<snp>.hr files (eval/idash.cpp:66-114) and
