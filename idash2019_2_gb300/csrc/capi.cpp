@@ -51,11 +51,12 @@ struct Candidate {
     uint32_t w, g, slots, terms, groups, cps;
 };
 
-// Shared-memory carve-up of a window-kernel CTA for `cps` CTAs per SM.
-bool window_limits(const idash_ctx *ctx, uint32_t w, uint32_t cps, Candidate *c) {
+// Shared-memory carve-up of one buffer: a window-kernel CTA for `cps` CTAs
+// per SM, or one of the two buffers of a pipe-kernel CTA (one per SM).
+bool window_limits(const idash_ctx *ctx, KernelKind kind, uint32_t w, uint32_t cps, Candidate *c) {
     const size_t per_sm = 233472;  // 228 KB of shared memory per SM
-    size_t budget = per_sm / cps - kSmemReserve;
-    budget = std::min(budget, ctx->smem_optin);
+    size_t budget = std::min(per_sm / cps - kSmemReserve, ctx->smem_optin);
+    if (kind == KernelKind::kPipe) budget = (budget - 128) / 2;
     const uint32_t groups = 64;
     const size_t fixed = 128 + size_t(groups) * sizeof(PlanGroup);
     if (budget <= fixed) return false;
@@ -66,7 +67,7 @@ bool window_limits(const idash_ctx *ctx, uint32_t w, uint32_t cps, Candidate *c)
     uint32_t slots = uint32_t(left / (size_t(w) * 4));
     if (ctx->opt_max_window_slots > 0) slots = uint32_t(std::min<int64_t>(slots, ctx->opt_max_window_slots));
     if (slots == 0) return false;
-    *c = Candidate{KernelKind::kWindow, w, 3, slots, terms, groups, cps};
+    *c = Candidate{kind, w, 3, slots, terms, groups, kind == KernelKind::kPipe ? 1u : cps};
     return true;
 }
 
@@ -126,12 +127,13 @@ idash_status build_and_upload(idash_model *m, const Candidate &c) {
     m->max_terms = m->plan.max_block_terms;
     m->max_groups = m->plan.max_block_groups;
     uint32_t cps = c.cps;
-    if (c.kind == KernelKind::kWindow) {
-        const size_t smem = window_smem_bytes(c.w, m->max_slots, m->max_terms, m->max_groups);
-        const int occ = window_ctas_per_sm(c.w, c.g, smem);
-        if (occ <= 0) return ctx->fail(IDASH_ERR_CUDA, "window kernel cannot be resident with this shared memory");
+    if (c.kind != KernelKind::kDirect) {
+        const size_t smem = kernel_smem_bytes(c.kind, c.w, m->max_slots, m->max_terms, m->max_groups);
+        const int occ = resident_ctas_per_sm(c.kind, c.w, c.g, smem);
+        if (occ <= 0) return ctx->fail(IDASH_ERR_CUDA, "scoring kernel cannot be resident with this shared memory");
         cps = std::min<uint32_t>(cps ? cps : uint32_t(occ), uint32_t(occ));
-        if (ctx->opt_ctas_per_sm > 0) cps = std::min<uint32_t>(uint32_t(ctx->opt_ctas_per_sm), uint32_t(occ));
+        if (ctx->opt_ctas_per_sm > 0 && c.kind == KernelKind::kWindow)
+            cps = std::min<uint32_t>(uint32_t(ctx->opt_ctas_per_sm), uint32_t(occ));
     }
     m->ctas = uint32_t(ctx->sm_count) * std::max<uint32_t>(cps, 1);
     return IDASH_OK;
@@ -268,15 +270,19 @@ std::vector<Candidate> candidates(idash_model *m) {
     std::vector<uint32_t> ws;
     if (ctx->opt_slice_words) ws.push_back(uint32_t(ctx->opt_slice_words));
     else if (m->form == Form::kTrlwe) ws = {2048, 1024, 512};
-    else ws = {1024, 512, 256};
+    else ws = {1024, 512, 256, 128};
     std::vector<uint32_t> cpss;
     if (ctx->opt_ctas_per_sm > 0) cpss.push_back(uint32_t(ctx->opt_ctas_per_sm));
     else cpss = {1, 2};
-    for (uint32_t w : ws)
-        for (uint32_t cps : cpss) {
-            Candidate c;
-            if (window_limits(ctx, w, cps, &c)) out.push_back(c);
-        }
+    const bool window = ctx->opt_kernel == 0 || ctx->opt_kernel == 2;
+    const bool pipe = ctx->opt_kernel == 0 || ctx->opt_kernel == 3;
+    for (uint32_t w : ws) {
+        Candidate c;
+        if (window)
+            for (uint32_t cps : cpss)
+                if (window_limits(ctx, KernelKind::kWindow, w, cps, &c)) out.push_back(c);
+        if (pipe && window_limits(ctx, KernelKind::kPipe, w, 1, &c)) out.push_back(c);
+    }
     return out;
 }
 
@@ -287,7 +293,7 @@ idash_status plan_default(idash_model *m) {
         last = build_and_upload(m, c);
         if (last == IDASH_OK || last == IDASH_ERR_INDEX) return last;
     }
-    if (last == IDASH_ERR_UNSUPPORTED && m->ctx->opt_kernel == 0) {
+    if (last == IDASH_ERR_UNSUPPORTED && m->ctx->opt_kernel != 1) {
         // Neighbourhoods too large for any window: fall back to the direct kernel.
         Candidate c{KernelKind::kDirect, 512, 1, 0xFFFFFFFFu, 0xFFFFFFFFu, 8, 0};
         last = build_and_upload(m, c);
@@ -295,9 +301,7 @@ idash_status plan_default(idash_model *m) {
     return last;
 }
 
-bool autotune_wanted(const idash_model *m) {
-    return !m->tuned && m->ctx->opt_kernel == 0 && (m->ctx->opt_slice_words == 0 || m->ctx->opt_ctas_per_sm == 0);
-}
+bool autotune_wanted(idash_model *m) { return !m->tuned && m->ctx->opt_kernel != 1 && candidates(m).size() > 1; }
 
 }  // namespace
 
@@ -436,11 +440,11 @@ idash_status idash_set_option(idash_ctx *ctx, const char *name, int64_t value) {
     if (!ctx || !name) return IDASH_ERR_INVALID_ARGUMENT;
     const std::string n(name);
     if (n == "kernel") {
-        if (value != 0 && value != 1) return ctx->fail(IDASH_ERR_INVALID_ARGUMENT, "kernel must be 0 or 1");
+        if (value < 0 || value > 3) return ctx->fail(IDASH_ERR_INVALID_ARGUMENT, "kernel must be 0, 1, 2 or 3");
         ctx->opt_kernel = value;
     } else if (n == "slice_words") {
-        if (value != 0 && value != 256 && value != 512 && value != 1024 && value != 2048)
-            return ctx->fail(IDASH_ERR_INVALID_ARGUMENT, "slice_words must be 0, 256, 512, 1024 or 2048");
+        if (value != 0 && !slice_supported(uint32_t(value)))
+            return ctx->fail(IDASH_ERR_INVALID_ARGUMENT, "slice_words must be 0, 128, 256, 512, 1024 or 2048");
         ctx->opt_slice_words = value;
     } else if (n == "ctas_per_sm") {
         if (value < 0 || value > 8) return ctx->fail(IDASH_ERR_INVALID_ARGUMENT, "ctas_per_sm must be in [0, 8]");
@@ -600,7 +604,7 @@ idash_status idash_model_get_info(const idash_model *m, idash_model_info *info) 
     info->n_slots = m->plan.slots.size();
     info->slice_words = m->slice_words;
     info->max_window_slots = m->max_slots;
-    info->kernel = m->kind == KernelKind::kWindow ? 0u : 1u;
+    info->kernel = uint32_t(m->kind);
     info->algorithmic_in_rows = m->plan.distinct_rows;
     return IDASH_OK;
 }

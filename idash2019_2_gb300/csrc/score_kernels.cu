@@ -242,6 +242,143 @@ __global__ void __launch_bounds__(kThreads) k_score_window(const ScoreArgs a) {
     }
 }
 
+// Issues the bulk copies of one tile (terms, groups, unrotated slot slices)
+// into one buffer; called by warp 0, lane 0 arrives on the buffer's barrier.
+template <int W>
+__device__ __forceinline__ void issue_tile_loads(const ScoreArgs &a, const PlanBlock &blk, uint32_t c0,
+                                                 uint32_t copy_bytes, uint32_t *win, PlanTerm *terms_s,
+                                                 PlanGroup *groups_s, uint64_t *bar, uint32_t lane) {
+    if (lane == 0) fence_proxy_async_smem();
+    __syncwarp();
+    const uint32_t n_unrot = uint32_t(blk.n_slots) - blk.n_rot;
+    for (uint32_t s = lane; s < n_unrot; s += 32) {
+        const PlanSlot sl = a.slots[blk.slot_begin + s];
+        if (sl.row >= a.n_rows) {
+            report_error(a.err, kDevBadIndex);
+            continue;
+        }
+        mbar_expect_tx(bar, copy_bytes);
+        bulk_g2s(win + size_t(s) * W, a.in + uint64_t(sl.row) * a.in_stride + uint64_t(c0) * 4, copy_bytes, bar);
+    }
+    if (lane == 0) {
+        if (blk.n_terms) {
+            mbar_expect_tx(bar, blk.n_terms * uint32_t(sizeof(PlanTerm)));
+            bulk_g2s(terms_s, a.terms + blk.term_begin, blk.n_terms * uint32_t(sizeof(PlanTerm)), bar);
+        }
+        mbar_expect_tx(bar, blk.n_groups * uint32_t(sizeof(PlanGroup)));
+        bulk_g2s(groups_s, a.groups + blk.group_begin, blk.n_groups * uint32_t(sizeof(PlanGroup)), bar);
+    }
+    __syncwarp();
+    if (lane == 0) mbar_arrive(bar);
+}
+
+constexpr int kPipeThreads = 512;
+
+// k_score_pipe (batched, double-buffered): one 512-thread CTA per SM; while
+// all warps accumulate tile i from one shared-memory buffer, warp 0 has
+// already issued the bulk copies of tile i+1 into the other, so the input
+// window's load latency hides behind the previous tile's arithmetic.
+template <int W, int G, int Q>
+__global__ void __launch_bounds__(kPipeThreads, 1) k_score_pipe(const ScoreArgs a) {
+    constexpr int TEAM = W / (4 * Q);
+    constexpr int NTEAMS = kPipeThreads / TEAM;
+    static_assert(TEAM >= 32 && kPipeThreads % TEAM == 0, "a team is one or more whole warps");
+    extern __shared__ __align__(128) uint8_t smem[];
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem);  // bar[0], bar[1]
+    uint32_t *tile_s = reinterpret_cast<uint32_t *>(smem + 16);
+    const uint32_t buf_bytes = a.max_slots * W * 4 + a.max_terms * uint32_t(sizeof(PlanTerm)) +
+                               a.max_groups * uint32_t(sizeof(PlanGroup));
+    const uint32_t terms_off = a.max_slots * W * 4;
+    const uint32_t groups_off = terms_off + a.max_terms * uint32_t(sizeof(PlanTerm));
+    // buffer i: window at smem+128+i*buf_bytes, then terms, then groups
+    auto win_of = [&](uint32_t i) { return reinterpret_cast<uint32_t *>(smem + 128 + i * buf_bytes); };
+    auto terms_of = [&](uint32_t i) { return reinterpret_cast<PlanTerm *>(smem + 128 + i * buf_bytes + terms_off); };
+    auto groups_of = [&](uint32_t i) {
+        return reinterpret_cast<PlanGroup *>(smem + 128 + i * buf_bytes + groups_off);
+    };
+    const uint32_t tid = threadIdx.x;
+    if (tid == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        fence_mbar_init();
+        *tile_s = atomicAdd(a.tile_counter, 1u);
+    }
+    __syncthreads();
+    uint32_t cur = *tile_s;
+    const uint32_t team = tid / TEAM, lane = tid % TEAM;
+    uint32_t phase = 0;  // bit i: parity of the next completion of bar[i]
+    auto tile_geom = [&](uint32_t tile, PlanBlock &blk, uint32_t &c0, uint32_t &valid) {
+        blk = a.blocks[a.block_lo + tile % a.n_blocks];
+        c0 = (tile / a.n_blocks) * W;
+        valid = min(uint32_t(W), a.row_words - c0);
+    };
+    if (cur < a.n_tiles && tid < 32) {
+        PlanBlock blk;
+        uint32_t c0, valid;
+        tile_geom(cur, blk, c0, valid);
+        issue_tile_loads<W>(a, blk, c0, ((valid + 3u) & ~3u) * 4u, win_of(0), terms_of(0), groups_of(0), &bar[0], tid);
+    }
+    for (uint32_t i = 0; cur < a.n_tiles; ++i) {
+        const uint32_t b = i & 1u;
+        __syncthreads();  // every thread is done with buffer b^1 (tile i-1) and has read *tile_s
+        if (tid == 0) *tile_s = atomicAdd(a.tile_counter, 1u);
+        __syncthreads();
+        const uint32_t nxt = *tile_s;
+        if (nxt < a.n_tiles && tid < 32) {
+            PlanBlock nb;
+            uint32_t n0, nvalid;
+            tile_geom(nxt, nb, n0, nvalid);
+            issue_tile_loads<W>(a, nb, n0, ((nvalid + 3u) & ~3u) * 4u, win_of(b ^ 1u), terms_of(b ^ 1u),
+                                groups_of(b ^ 1u), &bar[b ^ 1u], tid);
+        }
+        PlanBlock blk;
+        uint32_t c0, valid;
+        tile_geom(cur, blk, c0, valid);
+        uint32_t *win = win_of(b);
+        if (blk.n_rot) {
+            for (uint32_t s = uint32_t(blk.n_slots) - blk.n_rot; s < blk.n_slots; ++s) {
+                const PlanSlot sl = a.slots[blk.slot_begin + s];
+                if (sl.row >= a.n_rows) continue;
+                const uint32_t *src = reinterpret_cast<const uint32_t *>(a.in + uint64_t(sl.row) * a.in_stride);
+                for (uint32_t x = tid; x < valid; x += kPipeThreads)
+                    win[size_t(s) * W + x] = rotated_word(src, c0 + x, sl.rot, a.N);
+            }
+            __syncthreads();
+        }
+        const bool ok = mbar_wait_bounded(&bar[b], (phase >> b) & 1u, a.err);
+        if (__syncthreads_or(!ok)) {
+            // drain: every copy this CTA issued must land before it exits
+            mbar_wait_bounded(&bar[b], (phase >> b) & 1u, nullptr);
+            if (nxt < a.n_tiles) mbar_wait_bounded(&bar[b ^ 1u], (phase >> (b ^ 1u)) & 1u, nullptr);
+            return;
+        }
+        phase ^= 1u << b;
+
+        uint32_t bias_mask, zero_mask;
+        column_masks<Q, TEAM>(a, c0, lane, bias_mask, zero_mask);
+        const uint32_t *wlane = win + 4 * lane;
+        const PlanTerm *terms_s = terms_of(b);
+        const PlanGroup *groups_s = groups_of(b);
+        for (uint32_t g = team; g < blk.n_groups; g += NTEAMS) {
+            const PlanGroup gr = groups_s[g];
+            uint32_t acc[G][4 * Q];
+            init_acc<G, Q>(acc, gr, bias_mask);
+            const PlanTerm *tp = terms_s + gr.term_begin;
+#pragma unroll 2
+            for (uint32_t t = 0; t < gr.n_terms; ++t) {
+                const PlanTerm tm = tp[t];
+                const uint32_t *w = wlane + size_t(tm.slot) * W;
+                uint4 x[Q];
+#pragma unroll
+                for (int k = 0; k < Q; ++k) x[k] = *reinterpret_cast<const uint4 *>(w + 4 * k * TEAM);
+                mac<G, Q>(acc, tm, x);
+            }
+            write_outputs<G, Q, TEAM>(a, gr, acc, c0, lane, valid, zero_mask);
+        }
+        cur = nxt;
+    }
+}
+
 template <int W, int G, int Q>
 __global__ void __launch_bounds__(kThreads) k_score_direct(const ScoreArgs a) {
     constexpr int TEAM = W / (4 * Q);
@@ -322,46 +459,85 @@ __global__ void k_finalize(const FinalizeArgs a) {
 
 using KernelFn = void (*)(const ScoreArgs);
 
-// Columns per thread: 16 (4 quads) from 512-word slices up, 8 below; the
-// direct kernel keeps 8 so that each output has 256 threads of loads in flight.
+// Columns per thread: 16 (4 quads) from 512-word slices up, 8 at 256 and 4 at
+// 128 (a team is always whole warps); the direct kernel keeps 8 (4 at 128)
+// so that each output has a full CTA of loads in flight.
 template <int G>
 KernelFn pick(KernelKind kind, uint32_t w) {
-    const bool win = kind == KernelKind::kWindow;
-    switch (w) {
-        case 256: return win ? k_score_window<256, G, 2> : k_score_direct<256, G, 2>;
-        case 512: return win ? k_score_window<512, G, 4> : k_score_direct<512, G, 2>;
-        case 1024: return win ? k_score_window<1024, G, 4> : k_score_direct<1024, G, 2>;
-        case 2048: return win ? k_score_window<2048, G, 4> : k_score_direct<2048, G, 2>;
-        default: return nullptr;
+    switch (kind) {
+        case KernelKind::kWindow:
+            switch (w) {
+                case 128: return k_score_window<128, G, 1>;
+                case 256: return k_score_window<256, G, 2>;
+                case 512: return k_score_window<512, G, 4>;
+                case 1024: return k_score_window<1024, G, 4>;
+                case 2048: return k_score_window<2048, G, 4>;
+            }
+            break;
+        case KernelKind::kPipe:
+            switch (w) {
+                case 128: return k_score_pipe<128, G, 1>;
+                case 256: return k_score_pipe<256, G, 2>;
+                case 512: return k_score_pipe<512, G, 4>;
+                case 1024: return k_score_pipe<1024, G, 4>;
+                case 2048: return k_score_pipe<2048, G, 4>;
+            }
+            break;
+        case KernelKind::kDirect:
+            switch (w) {
+                case 128: return k_score_direct<128, G, 1>;
+                case 256: return k_score_direct<256, G, 2>;
+                case 512: return k_score_direct<512, G, 2>;
+                case 1024: return k_score_direct<1024, G, 2>;
+                case 2048: return k_score_direct<2048, G, 2>;
+            }
+            break;
     }
+    return nullptr;
 }
 
 KernelFn pick_kernel(KernelKind kind, uint32_t w, uint32_t g) {
     return g == 1 ? pick<1>(kind, w) : g == 3 ? pick<3>(kind, w) : nullptr;
 }
 
+uint32_t threads_of(KernelKind kind) { return kind == KernelKind::kPipe ? kPipeThreads : kThreads; }
+
 }  // namespace
 
-size_t window_smem_bytes(uint32_t slice_words, uint32_t max_slots, uint32_t max_terms, uint32_t max_groups) {
-    return 128 + size_t(max_slots) * slice_words * 4 + size_t(max_terms) * sizeof(PlanTerm) +
+bool slice_supported(uint32_t w) { return w == 128 || w == 256 || w == 512 || w == 1024 || w == 2048; }
+
+size_t buffer_bytes(uint32_t slice_words, uint32_t max_slots, uint32_t max_terms, uint32_t max_groups) {
+    return size_t(max_slots) * slice_words * 4 + size_t(max_terms) * sizeof(PlanTerm) +
            size_t(max_groups) * sizeof(PlanGroup);
 }
 
+size_t kernel_smem_bytes(KernelKind kind, uint32_t slice_words, uint32_t max_slots, uint32_t max_terms,
+                         uint32_t max_groups) {
+    const size_t buf = buffer_bytes(slice_words, max_slots, max_terms, max_groups);
+    switch (kind) {
+        case KernelKind::kWindow: return 128 + buf;
+        case KernelKind::kPipe: return 128 + 2 * buf;
+        default: return 0;
+    }
+}
+
 cudaError_t configure_window_kernels(size_t max_smem) {
-    for (uint32_t w : {256u, 512u, 1024u, 2048u})
-        for (uint32_t g : {1u, 3u}) {
-            cudaError_t e = cudaFuncSetAttribute(pick_kernel(KernelKind::kWindow, w, g),
-                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, int(max_smem));
-            if (e != cudaSuccess) return e;
-        }
+    for (KernelKind kind : {KernelKind::kWindow, KernelKind::kPipe})
+        for (uint32_t w : {128u, 256u, 512u, 1024u, 2048u})
+            for (uint32_t g : {1u, 3u}) {
+                cudaError_t e = cudaFuncSetAttribute(pick_kernel(kind, w, g),
+                                                     cudaFuncAttributeMaxDynamicSharedMemorySize, int(max_smem));
+                if (e != cudaSuccess) return e;
+            }
     return cudaSuccess;
 }
 
-int window_ctas_per_sm(uint32_t slice_words, uint32_t group_size, size_t smem_bytes) {
-    KernelFn fn = pick_kernel(KernelKind::kWindow, slice_words, group_size);
-    if (!fn) return 0;
+int resident_ctas_per_sm(KernelKind kind, uint32_t slice_words, uint32_t group_size, size_t smem_bytes) {
+    KernelFn fn = pick_kernel(kind, slice_words, group_size);
+    if (!fn || kind == KernelKind::kDirect) return 0;
     int n = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, kThreads, smem_bytes) != cudaSuccess) return 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, int(threads_of(kind)), smem_bytes) != cudaSuccess)
+        return 0;
     return n;
 }
 
@@ -370,13 +546,13 @@ cudaError_t launch_score(KernelKind kind, uint32_t slice_words, uint32_t group_s
     KernelFn fn = pick_kernel(kind, slice_words, group_size);
     if (!fn) return cudaErrorInvalidValue;
     if (a.n_tiles == 0) return cudaSuccess;
-    if (kind == KernelKind::kWindow) {
-        const size_t smem = window_smem_bytes(slice_words, a.max_slots, a.max_terms, a.max_groups);
+    if (kind == KernelKind::kDirect) {
+        fn<<<a.n_tiles, kThreads, 0, stream>>>(a);
+    } else {
+        const size_t smem = kernel_smem_bytes(kind, slice_words, a.max_slots, a.max_terms, a.max_groups);
         cudaError_t e = cudaMemsetAsync(a.tile_counter, 0, sizeof(uint32_t), stream);
         if (e != cudaSuccess) return e;
-        fn<<<ctas < a.n_tiles ? ctas : a.n_tiles, kThreads, smem, stream>>>(a);
-    } else {
-        fn<<<a.n_tiles, kThreads, 0, stream>>>(a);
+        fn<<<ctas < a.n_tiles ? ctas : a.n_tiles, threads_of(kind), smem, stream>>>(a);
     }
     return cudaGetLastError();
 }

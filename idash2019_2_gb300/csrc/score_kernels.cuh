@@ -36,22 +36,38 @@ struct ScoreArgs {
     uint32_t *err;                // device error word
 };
 
-enum class KernelKind : int { kWindow = 0, kDirect = 1 };
+// kWindow: persistent, 256 threads, one shared-memory buffer, 1-2 CTAs/SM.
+// kDirect: one CTA per tile, inputs read from global memory (plain form).
+// kPipe:   persistent, 512 threads, two buffers (next tile loads while the
+//          current one computes), one CTA per SM.
+enum class KernelKind : int { kWindow = 0, kDirect = 1, kPipe = 2 };
 
-// Shared memory a window-kernel CTA needs for the given limits.
-size_t window_smem_bytes(uint32_t slice_words, uint32_t max_slots, uint32_t max_terms, uint32_t max_groups);
+// Slice widths the kernels are instantiated for.
+bool slice_supported(uint32_t slice_words);
+
+// One shared-memory buffer (window + terms + groups) for the given limits.
+size_t buffer_bytes(uint32_t slice_words, uint32_t max_slots, uint32_t max_terms, uint32_t max_groups);
+// Dynamic shared memory of one CTA of `kind` (0 for the direct kernel).
+size_t kernel_smem_bytes(KernelKind kind, uint32_t slice_words, uint32_t max_slots, uint32_t max_terms,
+                         uint32_t max_groups);
+inline size_t window_smem_bytes(uint32_t slice_words, uint32_t max_slots, uint32_t max_terms, uint32_t max_groups) {
+    return kernel_smem_bytes(KernelKind::kWindow, slice_words, max_slots, max_terms, max_groups);
+}
 
 // Launches one scoring kernel.  `ctas` is the persistent grid size (window
-// kernel) and is ignored by the direct kernel (one CTA per tile).
+// and pipe kernels) and is ignored by the direct kernel (one CTA per tile).
 cudaError_t launch_score(KernelKind kind, uint32_t slice_words, uint32_t group_size, const ScoreArgs &a,
                          uint32_t ctas, cudaStream_t stream);
 
-// Allows every window-kernel instance up to `max_smem` bytes of dynamic
-// shared memory (once per context, before any launch or capture).
+// Allows every persistent kernel instance up to `max_smem` bytes of dynamic
+// shared memory (once per device, before any launch or capture).
 cudaError_t configure_window_kernels(size_t max_smem);
 
-// Largest resident CTA count per SM for the window kernel at this smem size.
-int window_ctas_per_sm(uint32_t slice_words, uint32_t group_size, size_t smem_bytes);
+// Largest resident CTA count per SM for a persistent kernel at this smem size.
+int resident_ctas_per_sm(KernelKind kind, uint32_t slice_words, uint32_t group_size, size_t smem_bytes);
+inline int window_ctas_per_sm(uint32_t slice_words, uint32_t group_size, size_t smem_bytes) {
+    return resident_ctas_per_sm(KernelKind::kWindow, slice_words, group_size, smem_bytes);
+}
 
 struct FinalizeArgs {
     const uint64_t *var_ptr;

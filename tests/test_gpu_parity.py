@@ -92,16 +92,18 @@ def test_trlwe_synth_vs_oracle(ctx, oracle, regions, kernel):
     np.testing.assert_array_equal(got, want)
 
 
-@pytest.mark.parametrize("slice_words", [256, 512, 1024, 2048])
-@pytest.mark.parametrize("graph", [0, 1])
-def test_trlwe_device_path_tiles(ctx, oracle, slice_words, graph):
-    """Every slice width of the window kernel, with and without graph replay,
-    on the device-resident path (dense rows)."""
+@pytest.mark.parametrize("slice_words", [128, 256, 512, 1024, 2048])
+@pytest.mark.parametrize("kernel,graph", [(2, 0), (2, 1), (3, 1)])
+def test_trlwe_device_path_tiles(ctx, oracle, slice_words, kernel, graph):
+    """Every slice width of the single-buffer (2) and double-buffer (3)
+    persistent kernels, with and without graph replay, on the
+    device-resident path (dense rows)."""
     w = gpu.synth_model(seed=3, n_tags=200, n_targets=700, choices=[5, 2, 3, 1])
     n_rows = 600
     rows = random_rows(5, n_rows)
     ctx.set_option("slice_words", slice_words)
     ctx.set_option("graph", graph)
+    ctx.set_option("kernel", kernel)
     try:
         m = gpu.TrlweModel(ctx, w.model, n_rows, 1000, 1, 1024)
         d_in = ctx.device_alloc(rows.nbytes)
@@ -116,10 +118,35 @@ def test_trlwe_device_path_tiles(ctx, oracle, slice_words, graph):
                                          1024)
             np.testing.assert_array_equal(got, want)
         assert m.info()["slice_words"] == slice_words
+        assert m.info()["kernel"] == (0 if kernel == 2 else 2)
         m.free()
     finally:
         ctx.set_option("slice_words", 0)
         ctx.set_option("graph", 1)
+        ctx.set_option("kernel", 0)
+
+
+@pytest.mark.parametrize("kernel", [2, 3])
+def test_trlwe_regions_persistent_kernels(ctx, oracle, kernel):
+    """NUM_REGIONS = 10 (rotated slots gathered in shared memory) on both
+    persistent kernels with a graph."""
+    w = gpu.synth_model(seed=17, n_tags=150, n_targets=400, neighbours=6)
+    n_rows = (3 * 150 + 9) // 10
+    rows = random_rows(17, n_rows)
+    ctx.set_option("kernel", kernel)
+    try:
+        m = gpu.TrlweModel(ctx, w.model, n_rows, 100, 10, 102)
+        d_in = ctx.device_alloc(rows.nbytes)
+        d_out = ctx.device_alloc(m.n_out * 8192)
+        d_in.upload(rows)
+        m.score_device(d_in.ptr, gpu.DENSE_TRLWE, d_out.ptr, gpu.DENSE_TRLWE)
+        ctx.sync()
+        got = d_out.download(dtype=np.int32).reshape(m.n_out, 2048)
+        m.free()
+    finally:
+        ctx.set_option("kernel", 0)
+    want, _ = oracle.trlwe_score(w.model.term_ptr, w.model.term_feat, w.model.term_coef, rows, 100, 10, 102)
+    np.testing.assert_array_equal(got, want)
 
 
 def test_large_neighbourhoods_fall_back_to_direct_kernel(ctx, oracle):
@@ -149,10 +176,11 @@ def test_trlwe_autotune_picks_a_correct_plan(ctx, oracle):
     np.testing.assert_array_equal(got, want)
     np.testing.assert_array_equal(got2, want)
     info = m.info()
-    assert info["kernel"] == 0 and info["slice_words"] in (512, 1024, 2048)
+    assert info["kernel"] in (0, 2) and info["slice_words"] in (512, 1024, 2048)
 
 
-def test_lwe_vs_oracle_ranges(ctx, oracle):
+@pytest.mark.parametrize("kernel,slice_words", [(0, 0), (2, 128), (3, 256), (3, 512), (1, 256)])
+def test_lwe_vs_oracle_ranges(ctx, oracle, kernel, slice_words):
     n, n_indiv, n_tags = 1024, 37, 60
     w = gpu.synth_model(seed=9, n_tags=n_tags, n_targets=90, choices=[5, 10, 2])
     n_feat = 3 * n_tags
@@ -161,19 +189,27 @@ def test_lwe_vs_oracle_ranges(ctx, oracle):
     gpu.synth_lwe_device(ctx, 77, n, n_indiv, n_feat, d_in.ptr, stride)
     ctx.sync()
     rows = d_in.download(dtype=np.int32).reshape(n_feat, stride)
-    m = gpu.LweModel(ctx, w.model, n_feat, n_indiv, n)
-    L = n_indiv * (n + 1)
-    for (lo, hi, ni) in [(0, m.n_out, n_indiv), (5, 131, n_indiv), (100, 101, n_indiv), (0, m.n_out, 11)]:
-        ostride = gpu.lwe_row_words(ni, n)
-        d_out = ctx.device_alloc((hi - lo) * ostride * 4)
-        m.score_device(ni, d_in.ptr, stride, lo, hi, d_out.ptr, ostride)
-        ctx.sync()
-        got = d_out.download(dtype=np.int32).reshape(hi - lo, ostride)[:, :ni * (n + 1)]
-        sub = rows if ni == n_indiv else np.ascontiguousarray(rows[:, :ni * (n + 1)])
-        want = oracle.lwe_score(w.model.term_ptr, w.model.term_feat, w.model.term_coef, sub, ni, lo, hi, n=n)
-        np.testing.assert_array_equal(got, want)
-        d_out.free()
-    assert L == rows.shape[1] - (stride - L)
+    ctx.set_option("kernel", kernel)
+    ctx.set_option("slice_words", slice_words)
+    try:
+        m = gpu.LweModel(ctx, w.model, n_feat, n_indiv, n)
+        for (lo, hi, ni) in [(0, m.n_out, n_indiv), (5, 131, n_indiv), (100, 101, n_indiv), (0, m.n_out, 11)]:
+            ostride = gpu.lwe_row_words(ni, n)
+            d_out = ctx.device_alloc((hi - lo) * ostride * 4)
+            m.score_device(ni, d_in.ptr, stride, lo, hi, d_out.ptr, ostride)
+            ctx.sync()
+            got = d_out.download(dtype=np.int32).reshape(hi - lo, ostride)[:, :ni * (n + 1)]
+            sub = rows if ni == n_indiv else np.ascontiguousarray(rows[:, :ni * (n + 1)])
+            want = oracle.lwe_score(w.model.term_ptr, w.model.term_feat, w.model.term_coef, sub, ni, lo, hi, n=n)
+            np.testing.assert_array_equal(got, want)
+            d_out.free()
+        if slice_words:
+            assert m.info()["slice_words"] == slice_words
+        m.free()
+    finally:
+        ctx.set_option("kernel", 0)
+        ctx.set_option("slice_words", 0)
+    d_in.free()
 
 
 def test_synth_lwe_matches_oracle_generator(ctx, oracle):
