@@ -265,6 +265,55 @@ def section_lwe(ctx, name, seed, n_indiv, n_tags, n_targets, neighbours=5, choic
     return out
 
 
+def section_serving(ctx, seed, n_requests=10000, budget=150 << 30, inflight=4):
+    """Continuous batching (idash_serve_trlwe) over a Poisson stream: each
+    request has individuals ~ U[1, 2000] and a contiguous target range of
+    length ~ U[1000, 80882]; 10 neighbours; model and index tables resident;
+    150 GB HBM admission budget.  The arrival rate is 0.8 x the measured
+    capacity (64 requests arriving at once)."""
+    import numpy as np
+    from idash2019_2_gb300 import gpu
+    T = 80882
+    w = gpu.synth_model(seed, 16184, T, neighbours=10)
+    m = gpu.TrlweModel(ctx, w.model, 3 * 16184, 1024, 1, 1024)
+    rng = np.random.default_rng(seed)
+
+    def draw(k):
+        out = []
+        for i in range(k):
+            length = int(rng.integers(1000, T + 1))
+            t0 = int(rng.integers(0, T - length + 1))
+            out.append(dict(arrival_s=0.0, n_indiv=int(rng.integers(1, 2001)), target_begin=t0,
+                            target_end=t0 + length, seed=int(rng.integers(1, 2 ** 62))))
+        return out
+
+    calib = draw(64)
+    res, _ = m.serve(calib, budget, inflight)  # includes the one-off autotune
+    res, _ = m.serve(calib, budget, inflight)
+    capacity = len(calib) / max(r["done_s"] for r in res)
+    rate = 0.8 * capacity
+    reqs = draw(n_requests)
+    t = np.cumsum(rng.exponential(1.0 / rate, size=n_requests))
+    for r, a in zip(reqs, t):
+        r["arrival_s"] = float(a)
+    t0 = time.perf_counter()
+    res, _ = m.serve(reqs, budget, inflight)
+    wall = time.perf_counter() - t0
+    lat = np.array([r["done_s"] - q["arrival_s"] for r, q in zip(res, reqs)])
+    makespan = max(r["done_s"] for r in res) - reqs[0]["arrival_s"]
+    preds = sum(q["n_indiv"] * (q["target_end"] - q["target_begin"]) * 3 for q in reqs)
+    m.free()
+    return {"value": preds / makespan, "unit": UNIT, "requests": n_requests, "requests_per_s": n_requests / makespan,
+            "p50_latency_ms": float(np.percentile(lat, 50) * 1e3), "p99_latency_ms": float(np.percentile(lat, 99) * 1e3),
+            "mean_latency_ms": float(lat.mean() * 1e3), "arrival_rate_per_s": rate,
+            "capacity_per_s": capacity, "hbm_budget_bytes": budget, "max_inflight": inflight,
+            "mean_request_device_bytes": float(np.mean([r["device_bytes"] for r in res])),
+            "wall_s": wall,
+            "workload": "Poisson stream of 10,000 requests: individuals ~ U[1,2000] (TRLWE-packed, 1,024 per "
+                        "block), contiguous targets of length ~ U[1000, 80882], 10 neighbours, 150 GB HBM budget; "
+                        "request ciphertexts generated on the device"}
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -376,6 +425,8 @@ def run_ours(args):
                                                    "individuals x 80,882 targets x 3, neighbours uniform from "
                                                    "{5,10,20,30,50}", args.seed + 1, 1000, 16184, 80882,
                                               choices=[5, 10, 20, 30, 50], passes=1)
+    if world == 1 and "serving" in sections:
+        forms["serving"] = section_serving(ctx, args.seed + 2)
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -407,7 +458,7 @@ def main():
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="trlwe_full")
     ap.add_argument("--seed", type=int, default=0x1DA52019)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--sections", default="plain,lwe_full,batched_uneven",
+    ap.add_argument("--sections", default="plain,lwe_full,batched_uneven,serving",
                     help="extra forms measured after the headline (comma list, '' for none)")
     args = ap.parse_args()
     args.steps_given = args.steps is not None

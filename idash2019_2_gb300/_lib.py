@@ -76,6 +76,20 @@ class SynthModel(C.Structure):
                 ("window_len", u32p)]
 
 
+class Request(C.Structure):
+    _fields_ = [("arrival_s", C.c_double), ("n_indiv", C.c_uint32), ("reserved", C.c_uint32),
+                ("target_begin", C.c_uint64), ("target_end", C.c_uint64), ("seed", C.c_uint64)]
+
+
+class RequestResult(C.Structure):
+    _fields_ = [("admit_s", C.c_double), ("done_s", C.c_double), ("device_bytes", C.c_uint64),
+                ("digest", C.c_uint64)]
+
+
+class ServeConfig(C.Structure):
+    _fields_ = [("hbm_budget", C.c_uint64), ("max_inflight", C.c_uint32), ("reserved", C.c_uint32)]
+
+
 class CloudReport(C.Structure):
     _fields_ = [("read_s", C.c_double), ("plan_s", C.c_double), ("score_s", C.c_double),
                 ("write_s", C.c_double), ("n_in_records", C.c_uint64), ("n_out_records", C.c_uint64)]
@@ -108,6 +122,14 @@ PROTOTYPES = {
                                    C.c_uint64]),
     "idash_score_lwe_device": (status_t, [vp, C.c_uint32, vp, C.c_uint64, C.c_uint64, C.c_uint64, vp,
                                           C.c_uint64, vp]),
+    "idash_score_trlwe_range": (status_t, [vp, C.c_uint64, C.c_uint64, C.c_uint32, vp, C.POINTER(RowLayout),
+                                           C.c_uint64, C.c_uint64, vp, C.POINTER(RowLayout), vp]),
+    "idash_model_input_rows": (status_t, [vp, C.c_uint64, C.c_uint64, u64p, u64p]),
+    "idash_serve_trlwe": (status_t, [vp, C.POINTER(ServeConfig), C.POINTER(Request), C.c_uint64,
+                                     C.POINTER(RequestResult), C.POINTER(vp)]),
+    "idash_digest_host": (C.c_uint64, [u32p, C.c_uint64, C.c_uint64]),
+    "idash_synth_uniform_device": (status_t, [vp, C.c_uint64, C.c_uint64, C.c_uint64, C.c_uint32, vp, C.c_uint64,
+                                              vp]),
     "idash_model_get_info": (status_t, [vp, C.POINTER(ModelInfo)]),
     "idash_model_replan": (status_t, [vp]),
     "idash_model_free": (None, [vp]),

@@ -805,6 +805,76 @@ idash_status idash_score_trlwe_host(idash_model *m, const void *h_in, const idas
     return idash_sync(ctx);
 }
 
+idash_status idash_model_input_rows(const idash_model *m, uint64_t out_begin, uint64_t out_end, uint64_t *row_begin,
+                                    uint64_t *row_end) {
+    if (!m || !row_begin || !row_end || out_begin > out_end || out_end > m->n_out) return IDASH_ERR_INVALID_ARGUMENT;
+    uint32_t b_lo, b_hi;
+    block_range(m, out_begin, out_end, &b_lo, &b_hi);
+    uint64_t lo = UINT64_MAX, hi = 0;
+    for (uint32_t b = b_lo; b < b_hi; ++b) {
+        if (m->plan.blocks[b].n_slots == 0) continue;
+        lo = std::min<uint64_t>(lo, m->plan.block_min_row[b]);
+        hi = std::max<uint64_t>(hi, uint64_t(m->plan.block_max_row[b]) + 1);
+    }
+    if (lo == UINT64_MAX) lo = hi = 0;
+    *row_begin = lo;
+    *row_end = hi;
+    return IDASH_OK;
+}
+
+idash_status idash_score_trlwe_range(idash_model *m, uint64_t out_begin, uint64_t out_end, uint32_t num_samples,
+                                     const void *d_in, const idash_row_layout *il, uint64_t in_row_base,
+                                     uint64_t n_in_rows, void *d_out, const idash_row_layout *ol, void *stream) {
+    if (!m || !d_in || !d_out || !il || !ol) return IDASH_ERR_INVALID_ARGUMENT;
+    idash_ctx *ctx = m->ctx;
+    if (m->form != Form::kTrlwe) return ctx->fail(IDASH_ERR_STATE, "model is not a TRLWE model");
+    if (out_begin > out_end || out_end > m->n_out) return ctx->fail(IDASH_ERR_INVALID_ARGUMENT, "bad output range");
+    if (num_samples > m->tp.region_size)
+        return ctx->fail(IDASH_ERR_INVALID_ARGUMENT, "num_samples must not exceed REGION_SIZE");
+    if (in_row_base > 0xFFFFFFFFull || n_in_rows > 0xFFFFFFFFull)
+        return ctx->fail(IDASH_ERR_INVALID_ARGUMENT, "input rows beyond 32-bit indices");
+    const uint64_t payload = uint64_t(2) * m->tp.N * 4;
+    idash_status s = check_layout(ctx, d_in, il, payload, false);
+    if (s == IDASH_OK) s = check_layout(ctx, d_out, ol, payload, true);
+    if (s != IDASH_OK) return s;
+    if (out_begin == out_end) return IDASH_OK;
+    uint64_t r_lo, r_hi;
+    idash_model_input_rows(m, out_begin, out_end, &r_lo, &r_hi);
+    if (r_hi > r_lo && (r_lo < in_row_base || r_hi > in_row_base + n_in_rows))
+        return ctx->fail(IDASH_ERR_INDEX, "the outputs read input rows outside [in_row_base, in_row_base + n_in_rows)");
+    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+    uint32_t b_lo, b_hi;
+    block_range(m, out_begin, out_end, &b_lo, &b_hi);
+    const uint8_t *in = static_cast<const uint8_t *>(d_in);
+    uint8_t *out = static_cast<uint8_t *>(d_out);
+    ScoreArgs a = make_args(m, in + il->payload_offset, il->row_stride, out + ol->payload_offset, ol->row_stride,
+                            row_words_of(m, 0), b_lo, b_hi, out_begin, out_end, out_begin);
+    a.out_row_map = nullptr;
+    a.row_base = uint32_t(in_row_base);
+    a.n_rows = uint32_t(n_in_rows);
+    if (num_samples) a.num_samples = num_samples;
+    if ((s = launch(m, a, st)) != IDASH_OK) return s;
+    FinalizeArgs f{};
+    f.var_ptr = m->d_var_ptr;
+    f.var_row = m->d_var_row;
+    f.var_coef = m->d_var_coef;
+    f.out_index = m->d_out_index;
+    f.out_row_map = nullptr;
+    f.o_begin = out_begin;
+    f.o_end = out_end;
+    f.in_rows = in;
+    f.in_row_base = uint32_t(in_row_base);
+    f.in_stride = il->row_stride;
+    f.in_var_off = il->variance_offset;
+    f.out_rows = out;
+    f.out_row_base = out_begin;
+    f.out_stride = ol->row_stride;
+    f.out_var_off = ol->variance_offset;
+    f.out_hdr_off = ol->header_offset;
+    f.tag = m->tp.record_tag;
+    return ctx->check_cuda(launch_finalize(f, st), "finalize launch");
+}
+
 idash_status idash_score_lwe_device(idash_model *m, uint32_t n_indiv, const int32_t *d_in, uint64_t in_row_stride,
                                     uint64_t out_begin, uint64_t out_end, int32_t *d_out, uint64_t out_row_stride,
                                     void *stream) {

@@ -12,6 +12,22 @@
 #include "plan.hpp"
 #include "score_kernels.cuh"
 
+namespace idash {
+// Synthetic TRLWE rows [row_begin, row_end) of the generator behind
+// idash_synth_trlwe_device, written to d_out (row row_begin at d_out).
+cudaError_t synth_trlwe_rows(uint64_t seed, const idash_trlwe_params &p, uint64_t n_features, uint64_t row_begin,
+                             uint64_t row_end, uint8_t *d_out, const idash_row_layout &layout, cudaStream_t s);
+// Uniformly random rows [row_begin, row_begin + n_rows) of row_words words
+// (as idash_synth_uniform_device), row row_begin at d_out.
+cudaError_t fill_uniform_rows(uint64_t seed, uint64_t row_begin, uint64_t n_rows, uint32_t row_words, uint8_t *d_out,
+                              uint64_t row_stride, int sm_count, cudaStream_t s);
+// Adds to *d_digest the order-independent digest of n_words output words
+// (sum mod 2^64 of mix64(index << 32 | word), index = index_base + i).
+cudaError_t digest_words(const uint32_t *words, uint64_t n_words, uint64_t index_base, uint64_t *d_digest,
+                         int sm_count, cudaStream_t s);
+uint64_t digest_host(const uint32_t *words, uint64_t n_words, uint64_t index_base);
+}  // namespace idash
+
 // Message returned by idash_last_error(NULL) on this thread (entry points
 // that have no context: idash_open failures, idash_score_trlwe_noalloc).
 void idash_set_thread_error(const std::string &msg);

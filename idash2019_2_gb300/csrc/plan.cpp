@@ -192,12 +192,14 @@ std::string build_plan(const PlanInput &in, const PlanLimits &lim, Plan *plan, b
         };
         b.n_slots = uint16_t(win.size());
         b.n_rot = uint16_t(win.size() - n_unrot);
-        uint32_t max_row = 0;
+        uint32_t max_row = 0, min_row = win.empty() ? 0u : 0xFFFFFFFFu;
         for (uint64_t k : win) {
             plan->slots.push_back(PlanSlot{uint32_t(k >> 32), uint32_t(k & 0xFFFFFFFFu)});
             max_row = std::max(max_row, uint32_t(k >> 32));
+            min_row = std::min(min_row, uint32_t(k >> 32));
         }
         plan->block_max_row.push_back(max_row);
+        plan->block_min_row.push_back(min_row);
         b.out_lo = uint32_t(groups[gi].o0);
         b.out_hi = uint32_t(groups[gend - 1].o0 + groups[gend - 1].n);
         for (size_t q = gi; q < gend; ++q) {

@@ -91,6 +91,7 @@ struct Plan {
     uint64_t distinct_rows = 0;    // input rows read at least once
     uint32_t max_row_per_block_hint = 0;
     std::vector<uint32_t> block_max_row;  // per block: largest input row read
+    std::vector<uint32_t> block_min_row;  // per block: smallest input row read (0 if none)
 };
 
 // Returns "" on success, else a message; *index_error is set when a term

@@ -180,12 +180,12 @@ __global__ void __launch_bounds__(kThreads) k_score_window(const ScoreArgs a) {
             const uint32_t n_unrot = uint32_t(blk.n_slots) - blk.n_rot;
             for (uint32_t s = tid; s < n_unrot; s += 32) {
                 const PlanSlot sl = a.slots[blk.slot_begin + s];
-                if (sl.row >= a.n_rows) {
+                if (sl.row - a.row_base >= a.n_rows) {
                     report_error(a.err, kDevBadIndex);
                     continue;
                 }
                 mbar_expect_tx(bar, copy_bytes);
-                bulk_g2s(win + size_t(s) * W, a.in + uint64_t(sl.row) * a.in_stride + uint64_t(c0) * 4, copy_bytes,
+                bulk_g2s(win + size_t(s) * W, a.in + uint64_t(sl.row - a.row_base) * a.in_stride + uint64_t(c0) * 4, copy_bytes,
                          bar);
             }
             if (tid == 0) {
@@ -203,8 +203,8 @@ __global__ void __launch_bounds__(kThreads) k_score_window(const ScoreArgs a) {
         if (blk.n_rot) {
             for (uint32_t s = uint32_t(blk.n_slots) - blk.n_rot; s < blk.n_slots; ++s) {
                 const PlanSlot sl = a.slots[blk.slot_begin + s];
-                if (sl.row >= a.n_rows) continue;
-                const uint32_t *src = reinterpret_cast<const uint32_t *>(a.in + uint64_t(sl.row) * a.in_stride);
+                if (sl.row - a.row_base >= a.n_rows) continue;
+                const uint32_t *src = reinterpret_cast<const uint32_t *>(a.in + uint64_t(sl.row - a.row_base) * a.in_stride);
                 for (uint32_t x = tid; x < valid; x += kThreads)
                     win[size_t(s) * W + x] = rotated_word(src, c0 + x, sl.rot, a.N);
             }
@@ -253,12 +253,12 @@ __device__ __forceinline__ void issue_tile_loads(const ScoreArgs &a, const PlanB
     const uint32_t n_unrot = uint32_t(blk.n_slots) - blk.n_rot;
     for (uint32_t s = lane; s < n_unrot; s += 32) {
         const PlanSlot sl = a.slots[blk.slot_begin + s];
-        if (sl.row >= a.n_rows) {
+        if (sl.row - a.row_base >= a.n_rows) {
             report_error(a.err, kDevBadIndex);
             continue;
         }
         mbar_expect_tx(bar, copy_bytes);
-        bulk_g2s(win + size_t(s) * W, a.in + uint64_t(sl.row) * a.in_stride + uint64_t(c0) * 4, copy_bytes, bar);
+        bulk_g2s(win + size_t(s) * W, a.in + uint64_t(sl.row - a.row_base) * a.in_stride + uint64_t(c0) * 4, copy_bytes, bar);
     }
     if (lane == 0) {
         if (blk.n_terms) {
@@ -338,8 +338,8 @@ __global__ void __launch_bounds__(kPipeThreads, 1) k_score_pipe(const ScoreArgs 
         if (blk.n_rot) {
             for (uint32_t s = uint32_t(blk.n_slots) - blk.n_rot; s < blk.n_slots; ++s) {
                 const PlanSlot sl = a.slots[blk.slot_begin + s];
-                if (sl.row >= a.n_rows) continue;
-                const uint32_t *src = reinterpret_cast<const uint32_t *>(a.in + uint64_t(sl.row) * a.in_stride);
+                if (sl.row - a.row_base >= a.n_rows) continue;
+                const uint32_t *src = reinterpret_cast<const uint32_t *>(a.in + uint64_t(sl.row - a.row_base) * a.in_stride);
                 for (uint32_t x = tid; x < valid; x += kPipeThreads)
                     win[size_t(s) * W + x] = rotated_word(src, c0 + x, sl.rot, a.N);
             }
@@ -404,11 +404,11 @@ __global__ void __launch_bounds__(kThreads) k_score_direct(const ScoreArgs a) {
         for (uint32_t t = 0; t < gr.n_terms; ++t) {
             const PlanTerm tm = tp[t];
             const PlanSlot sl = a.slots[blk.slot_begin + tm.slot];
-            if (sl.row >= a.n_rows) {
+            if (sl.row - a.row_base >= a.n_rows) {
                 report_error(a.err, kDevBadIndex);
                 continue;
             }
-            const uint8_t *src = a.in + uint64_t(sl.row) * a.in_stride;
+            const uint8_t *src = a.in + uint64_t(sl.row - a.row_base) * a.in_stride;
             uint4 x[Q];
 #pragma unroll
             for (int k = 0; k < Q; ++k) {
@@ -436,7 +436,7 @@ __global__ void __launch_bounds__(kThreads) k_score_direct(const ScoreArgs a) {
 __global__ void k_finalize(const FinalizeArgs a) {
     const uint64_t o = a.o_begin + uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (o >= a.o_end) return;
-    uint8_t *row = a.out_rows + (a.out_row_map ? uint64_t(a.out_row_map[o]) : o) * a.out_stride;
+    uint8_t *row = a.out_rows + (a.out_row_map ? uint64_t(a.out_row_map[o]) : o - a.out_row_base) * a.out_stride;
     if (a.out_hdr_off >= 0) {
         *reinterpret_cast<uint32_t *>(row + a.out_hdr_off) = a.out_index ? a.out_index[o] : uint32_t(o);
         *reinterpret_cast<int32_t *>(row + a.out_hdr_off + 4) = a.tag;
@@ -449,7 +449,8 @@ __global__ void k_finalize(const FinalizeArgs a) {
             for (uint64_t t = a.var_ptr[o]; t < a.var_ptr[o + 1]; ++t) {
                 const int64_t c = a.var_coef[t];
                 const double vin =
-                    *reinterpret_cast<const double *>(a.in_rows + uint64_t(a.var_row[t]) * a.in_stride + a.in_var_off);
+                    *reinterpret_cast<const double *>(a.in_rows + uint64_t(a.var_row[t] - a.in_row_base) * a.in_stride +
+                                                      a.in_var_off);
                 v = __dadd_rn(v, __dmul_rn(double(c * c), vin));
             }
         }

@@ -20,7 +20,8 @@ struct ScoreArgs {
     uint32_t n_slices;            // column slices per row
     uint32_t row_words;           // valid int32 words per row
     uint32_t n_tiles;             // n_blocks * n_slices
-    uint32_t n_rows;              // input rows (bounds guard)
+    uint32_t n_rows;              // input rows held at `in` (bounds guard)
+    uint32_t row_base;            // plan row r is held at row (r - row_base) of `in`
     const uint8_t *in;            // coefficient 0 of input row 0
     uint64_t in_stride;           // bytes
     uint8_t *out;                 // coefficient 0 of output row 0
@@ -77,9 +78,11 @@ struct FinalizeArgs {
     const uint32_t *out_row_map;  // may be null: row = o
     uint64_t o_begin, o_end;    // outputs finalised: [o_begin, o_end)
     const uint8_t *in_rows;     // input row 0 start (record start, not payload)
+    uint32_t in_row_base;       // plan row r is at row (r - in_row_base) of in_rows
     uint64_t in_stride;
     int64_t in_var_off;         // -1: inputs carry no variance (outputs get 0)
     uint8_t *out_rows;          // output row 0 start
+    uint64_t out_row_base;      // without a map, output o is row (o - out_row_base)
     uint64_t out_stride;
     int64_t out_var_off, out_hdr_off;
     int32_t tag;

@@ -81,16 +81,16 @@ __global__ void k_synth_lwe(uint64_t seed, uint32_t n, uint32_t n_indiv, uint64_
 // One CTA per TRLWE row: a uniform, b = a*s + e + m mod X^N+1 where m holds
 // the one-hot bit of feature row*R + r for individual s at slot r*RS + s.
 __global__ void k_synth_trlwe(uint64_t seed, uint32_t N, uint32_t num_samples, uint32_t num_regions,
-                              uint32_t region_size, uint32_t n_features, uint8_t *base, uint64_t stride,
-                              uint64_t payload_off, int64_t var_off, int64_t hdr_off, int32_t tag, int32_t one,
-                              double variance) {
+                              uint32_t region_size, uint32_t n_features, uint64_t row_begin, uint8_t *base,
+                              uint64_t stride, uint64_t payload_off, int64_t var_off, int64_t hdr_off, int32_t tag,
+                              int32_t one, double variance) {
     extern __shared__ uint32_t sh[];
     uint32_t *a = sh;          // N words
     uint32_t *key = sh + N;    // N words (0/1)
-    const uint64_t row = blockIdx.x;
+    const uint64_t row = row_begin + blockIdx.x;  // global row; stored at blockIdx.x
     const uint64_t key_s = stream_key(seed, 1), key_g = stream_key(seed, 2), key_a = stream_key(seed, 5),
                    key_e = stream_key(seed, 6);
-    uint8_t *rec = base + row * stride;
+    uint8_t *rec = base + uint64_t(blockIdx.x) * stride;
     uint32_t *out = reinterpret_cast<uint32_t *>(rec + payload_off);
     for (uint32_t j = threadIdx.x; j < N; j += blockDim.x) {
         a[j] = hash32k(key_a, row * N + j);
@@ -124,7 +124,70 @@ __global__ void k_synth_trlwe(uint64_t seed, uint32_t N, uint32_t num_samples, u
     }
 }
 
+// Order-independent digest of a request's output words: the sum mod 2^64 of
+// mix64(index << 32 | word) over every word, accumulated into *digest.
+__global__ void k_digest(const uint32_t *words, uint64_t n_words, uint64_t index_base,
+                         unsigned long long *digest) {
+    uint64_t acc = 0;
+    for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n_words;
+         i += uint64_t(gridDim.x) * blockDim.x)
+        acc += mix64(((index_base + i) << 32) | words[i]);
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xFFFFFFFFu, acc, off);
+    if ((threadIdx.x & 31) == 0) atomicAdd(digest, (unsigned long long)acc);
+}
+
+// Uniformly random ciphertext rows (stream 7): word j of global row r is
+// hash(seed, 7, r * row_words + j).  Statistically the same as encryptions,
+// without their cost; used for serving requests.
+__global__ void k_fill_uniform(uint64_t seed, uint64_t row_begin, uint64_t n_rows, uint32_t row_words,
+                               uint8_t *base, uint64_t stride) {
+    const uint64_t key = stream_key(seed, 7);
+    const uint64_t total = n_rows * row_words;
+    for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < total;
+         i += uint64_t(gridDim.x) * blockDim.x) {
+        const uint64_t r = i / row_words, j = i % row_words;
+        reinterpret_cast<uint32_t *>(base + r * stride)[j] = hash32k(key, (row_begin + r) * row_words + j);
+    }
+}
+
 }  // namespace
+
+cudaError_t fill_uniform_rows(uint64_t seed, uint64_t row_begin, uint64_t n_rows, uint32_t row_words, uint8_t *d_out,
+                              uint64_t row_stride, int sm_count, cudaStream_t s) {
+    if (n_rows == 0) return cudaSuccess;
+    const uint64_t want = (n_rows * row_words + 255) / 256;
+    const uint32_t blocks = uint32_t(std::min<uint64_t>(want, uint64_t(sm_count) * 16));
+    k_fill_uniform<<<blocks, 256, 0, s>>>(seed, row_begin, n_rows, row_words, d_out, row_stride);
+    return cudaGetLastError();
+}
+
+cudaError_t synth_trlwe_rows(uint64_t seed, const idash_trlwe_params &p, uint64_t n_features, uint64_t row_begin,
+                             uint64_t row_end, uint8_t *d_out, const idash_row_layout &layout, cudaStream_t s) {
+    if (row_end <= row_begin) return cudaSuccess;
+    const size_t smem = size_t(2) * p.N * sizeof(uint32_t);
+    k_synth_trlwe<<<uint32_t(row_end - row_begin), 256, smem, s>>>(
+        seed, p.N, p.num_samples, p.num_regions, p.region_size, uint32_t(n_features), row_begin, d_out,
+        layout.row_stride, layout.payload_offset, layout.variance_offset, layout.header_offset, p.record_tag,
+        p.one_t32, 0x1p-50);
+    return cudaGetLastError();
+}
+
+cudaError_t digest_words(const uint32_t *words, uint64_t n_words, uint64_t index_base, uint64_t *d_digest,
+                         int sm_count, cudaStream_t s) {
+    if (n_words == 0) return cudaSuccess;
+    const uint64_t want = (n_words + 255) / 256;
+    const uint32_t blocks = uint32_t(std::min<uint64_t>(want, uint64_t(sm_count) * 8));
+    k_digest<<<blocks, 256, 0, s>>>(words, n_words, index_base, reinterpret_cast<unsigned long long *>(d_digest));
+    return cudaGetLastError();
+}
+
+uint64_t digest_host(const uint32_t *words, uint64_t n_words, uint64_t index_base) {
+    uint64_t acc = 0;
+    for (uint64_t i = 0; i < n_words; ++i) acc += mix64(((index_base + i) << 32) | words[i]);
+    return acc;
+}
+
 }  // namespace idash
 
 using namespace idash;
@@ -246,11 +309,18 @@ extern "C" idash_status idash_synth_trlwe_device(idash_ctx *ctx, uint64_t seed, 
     const uint64_t rows = (n_features + p->num_regions - 1) / p->num_regions;
     if (rows == 0) return IDASH_OK;
     if (rows >= (1ull << 31)) return IDASH_ERR_INVALID_ARGUMENT;
-    const size_t smem = size_t(2) * p->N * sizeof(uint32_t);
-    k_synth_trlwe<<<uint32_t(rows), 256, smem, s>>>(seed, p->N, p->num_samples, p->num_regions, p->region_size,
-                                                   uint32_t(n_features), static_cast<uint8_t *>(d_out),
-                                                   layout->row_stride, layout->payload_offset,
-                                                   layout->variance_offset, layout->header_offset, p->record_tag,
-                                                   p->one_t32, 0x1p-50);
-    return ctx->check_cuda(cudaGetLastError(), "k_synth_trlwe launch");
+    return ctx->check_cuda(synth_trlwe_rows(seed, *p, n_features, 0, rows, static_cast<uint8_t *>(d_out), *layout, s),
+                           "k_synth_trlwe launch");
+}
+
+
+extern "C" idash_status idash_synth_uniform_device(idash_ctx *ctx, uint64_t seed, uint64_t row_begin, uint64_t n_rows,
+                                                   uint32_t row_words, void *d_out, uint64_t row_stride,
+                                                   void *stream) {
+    if (!ctx || !d_out || row_words == 0 || row_stride < uint64_t(row_words) * 4 || row_stride % 4)
+        return IDASH_ERR_INVALID_ARGUMENT;
+    cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+    return ctx->check_cuda(fill_uniform_rows(seed, row_begin, n_rows, row_words, static_cast<uint8_t *>(d_out),
+                                             row_stride, ctx->sm_count, s),
+                           "k_fill_uniform launch");
 }

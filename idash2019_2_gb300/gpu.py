@@ -263,6 +263,37 @@ class TrlweModel:
             self.h, C.c_void_p(h_in_ptr), C.byref(in_layout), n_in_rows, C.c_void_p(h_out_ptr),
             C.byref(out_layout)))
 
+    def score_range(self, out_begin: int, out_end: int, num_samples: int, d_in: int, in_layout: RowLayout,
+                    in_row_base: int, n_in_rows: int, d_out: int, out_layout: RowLayout, stream=None):
+        self.ctx.check(self.ctx.lib.idash_score_trlwe_range(
+            self.h, out_begin, out_end, num_samples, C.c_void_p(d_in), C.byref(in_layout), in_row_base, n_in_rows,
+            C.c_void_p(d_out), C.byref(out_layout), C.c_void_p(stream) if stream else None))
+
+    def input_rows(self, out_begin: int, out_end: int) -> tuple[int, int]:
+        lo, hi = C.c_uint64(), C.c_uint64()
+        self.ctx.check(self.ctx.lib.idash_model_input_rows(self.h, out_begin, out_end, C.byref(lo), C.byref(hi)))
+        return lo.value, hi.value
+
+    def serve(self, requests, hbm_budget: int, max_inflight: int, keep_outputs: bool = False):
+        """Runs idash_serve_trlwe over `requests` (dicts with arrival_s,
+        n_indiv, target_begin, target_end, seed).  Returns (results, outputs);
+        outputs[i] is request i's int32 [blocks, outputs, 2N] array when
+        keep_outputs, else None."""
+        n = len(requests)
+        reqs = (_lib.Request * max(n, 1))()
+        for i, r in enumerate(requests):
+            reqs[i] = _lib.Request(r["arrival_s"], r["n_indiv"], 0, r["target_begin"], r["target_end"], r["seed"])
+        res = (_lib.RequestResult * max(n, 1))()
+        cfg = _lib.ServeConfig(hbm_budget, max_inflight, 0)
+        outs, ptrs = None, None
+        if keep_outputs:
+            rs = self.params.region_size
+            outs = [np.zeros(((r["n_indiv"] + rs - 1) // rs, 3 * (r["target_end"] - r["target_begin"]), 2 * self.N),
+                             np.int32) for r in requests]
+            ptrs = (C.c_void_p * max(n, 1))(*[o.ctypes.data for o in outs])
+        self.ctx.check(self.ctx.lib.idash_serve_trlwe(self.h, C.byref(cfg), reqs, n, res, ptrs))
+        return [{k: getattr(res[i], k) for k, _ in res[i]._fields_} for i in range(n)], outs
+
     def score(self, rows: np.ndarray) -> np.ndarray:
         """Convenience: dense int32 [n_rows, 2N] in -> [n_out, 2N] out, via the
         host-memory path."""
@@ -323,6 +354,17 @@ def synth_trlwe_device(ctx: Context, seed: int, params: TrlweParams, n_tags: int
                        layout: RowLayout):
     ctx.check(ctx.lib.idash_synth_trlwe_device(ctx.h, seed, C.byref(params), n_tags, C.c_void_p(d_out),
                                                C.byref(layout), None))
+
+
+def synth_uniform_device(ctx: Context, seed: int, row_begin: int, n_rows: int, row_words: int, d_out: int,
+                         row_stride: int):
+    ctx.check(ctx.lib.idash_synth_uniform_device(ctx.h, seed, row_begin, n_rows, row_words, C.c_void_p(d_out),
+                                                 row_stride, None))
+
+
+def request_block_seed(seed: int, block: int) -> int:
+    """Seed of individual block `block` of a serving request (idash_serve_trlwe)."""
+    return (seed * 0x9E3779B97F4A7C15 + block) & ((1 << 64) - 1)
 
 
 def synth_lwe_device(ctx: Context, seed: int, n: int, n_indiv: int, n_feat_rows: int, d_out: int,

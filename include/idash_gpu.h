@@ -152,6 +152,58 @@ idash_status idash_score_trlwe_device(idash_model *model, const void *d_in, cons
 idash_status idash_score_trlwe_host(idash_model *model, const void *h_in, const idash_row_layout *in_layout,
                                     uint64_t n_in_rows, void *h_out, const idash_row_layout *out_layout);
 
+/* Scores outputs [out_begin, out_end) only (e.g. the contiguous targets of
+ * one serving request): output o goes to row (o - out_begin) of d_out.  The
+ * input holds n_in_rows rows; plan row r (FeatIndex, or in_row_of_index's
+ * value) is read from row (r - in_row_base).  num_samples (0 = the model's)
+ * is the number of packed individuals that receive the bias.  Asynchronous
+ * on `stream` (NULL: the context's stream); no graph, no autotuning. */
+idash_status idash_score_trlwe_range(idash_model *model, uint64_t out_begin, uint64_t out_end, uint32_t num_samples,
+                                     const void *d_in, const idash_row_layout *in_layout, uint64_t in_row_base,
+                                     uint64_t n_in_rows, void *d_out, const idash_row_layout *out_layout,
+                                     void *stream);
+/* The input rows [row_begin, row_end) that outputs [out_begin, out_end) read. */
+idash_status idash_model_input_rows(const idash_model *model, uint64_t out_begin, uint64_t out_end,
+                                    uint64_t *row_begin, uint64_t *row_end);
+
+/* ------------------------------------------- serving (continuous batching)
+ * No counterpart in the reference (its cloud binary scores one batch per
+ * process).  Serves a stream of imputation requests against one resident
+ * TRLWE model planned with NUM_REGIONS = 1: a request is n_indiv individuals
+ * (packed REGION_SIZE per TRLWE block) and the targets
+ * [target_begin, target_end) (outputs 3*target_begin .. 3*target_end).
+ * Requests are admitted in arrival order while a stream slot is free and
+ * their device memory fits hbm_budget; admitted requests run concurrently.
+ * Each request's ciphertexts are generated on the device (block b of a
+ * request: idash_synth_uniform_device with seed = seed * 0x9E3779B97F4A7C15 + b,
+ * rows [row_begin, row_end) of idash_model_input_rows), scored, and digested. */
+typedef struct {
+    double arrival_s;                  /* seconds after the run starts */
+    uint32_t n_indiv;                  /* individuals in the request */
+    uint32_t reserved;
+    uint64_t target_begin, target_end; /* contiguous target SNPs */
+    uint64_t seed;                     /* the request's synthetic ciphertexts */
+} idash_request;
+typedef struct {
+    double admit_s;        /* admission, seconds after the start (host clock) */
+    double done_s;         /* device completion, seconds after the start (CUDA events) */
+    uint64_t device_bytes; /* HBM the request held while in flight */
+    uint64_t digest;       /* sum mod 2^64 of mix64(index << 32 | word) over its output words */
+} idash_request_result;
+typedef struct {
+    uint64_t hbm_budget;   /* device bytes the in-flight requests may hold together */
+    uint32_t max_inflight; /* concurrent requests (one stream each), 1..64 */
+    uint32_t reserved;
+} idash_serve_config;
+/* Runs the whole stream (requests sorted by arrival_s) and fills results[i].
+ * host_out (optional) receives request i's output rows (blocks x outputs x
+ * 2N int32) in host_out[i] when non-NULL.  A request larger than the budget
+ * fails with IDASH_ERR_ADMISSION before anything runs. */
+idash_status idash_serve_trlwe(idash_model *model, const idash_serve_config *config, const idash_request *requests,
+                               uint64_t n_requests, idash_request_result *results, void *const *host_out);
+/* Host restatement of the serving digest, for checking results. */
+uint64_t idash_digest_host(const uint32_t *words, uint64_t n_words, uint64_t index_base);
+
 /* ------------------------------------------- per-individual LWE scoring
  * Each individual's one-hot bit is its own LWE sample (n mask words + body).
  * Input row f holds n_indiv samples of (n+1) int32, row stride in words a
@@ -261,6 +313,11 @@ idash_status idash_synth_lwe_device(idash_ctx *ctx, uint64_t seed, uint32_t n, u
                                     uint64_t n_feat_rows, int32_t *d_out, uint64_t row_stride, void *stream);
 idash_status idash_synth_trlwe_device(idash_ctx *ctx, uint64_t seed, const idash_trlwe_params *params,
                                       uint32_t n_tags, void *d_out, const idash_row_layout *layout, void *stream);
+/* Uniformly random ciphertext rows (statistically the same as encryptions):
+ * word j of global row r = hash(seed, r * row_words + j); rows
+ * [row_begin, row_begin + n_rows) are written from d_out on. */
+idash_status idash_synth_uniform_device(idash_ctx *ctx, uint64_t seed, uint64_t row_begin, uint64_t n_rows,
+                                        uint32_t row_words, void *d_out, uint64_t row_stride, void *stream);
 
 #ifdef __cplusplus
 }

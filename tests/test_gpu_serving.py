@@ -1,0 +1,80 @@
+"""Serving (idash_serve_trlwe): continuous batching of imputation requests
+against one resident model.  Each request's result is the same alone and in
+the mix (bit for bit), the mix really overlaps requests on the device, the
+outputs match the oracle, and requests beyond the HBM budget are refused."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+gpu = pytest.importorskip("idash2019_2_gb300.gpu")
+
+
+@pytest.fixture(scope="module")
+def served():
+    ctx = gpu.Context(0)
+    w = gpu.synth_model(seed=77, n_tags=300, n_targets=1000, neighbours=10)
+    m = gpu.TrlweModel(ctx, w.model, 900, 1024, 1, 1024)
+    rng = np.random.default_rng(5)
+    reqs = []
+    for i in range(10):
+        length = int(rng.integers(20, 400))
+        t0 = int(rng.integers(0, 1000 - length))
+        reqs.append(dict(arrival_s=0.0003 * i, n_indiv=int(rng.integers(1, 2600)), target_begin=t0,
+                         target_end=t0 + length, seed=1000 + i))
+    res, outs = m.serve(reqs, hbm_budget=2 << 30, max_inflight=4, keep_outputs=True)
+    yield ctx, w, m, reqs, res, outs
+    ctx.close()
+
+
+def test_each_request_is_the_same_alone_and_in_the_mix(served):
+    ctx, w, m, reqs, res, outs = served
+    for i, r in enumerate(reqs):
+        res1, out1 = m.serve([dict(r, arrival_s=0.0)], hbm_budget=2 << 30, max_inflight=1, keep_outputs=True)
+        np.testing.assert_array_equal(outs[i], out1[0])
+        assert res[i]["digest"] == res1[0]["digest"]
+
+
+def test_digests_restate_on_the_host(served):
+    ctx, w, m, reqs, res, outs = served
+    lib = ctx.lib
+    import ctypes as C
+    for i in (0, 3):
+        words = np.ascontiguousarray(outs[i]).view(np.uint32).ravel()
+        d = lib.idash_digest_host(words.ctypes.data_as(C.POINTER(C.c_uint32)), words.size, 0)
+        assert d == res[i]["digest"]
+
+
+def test_the_mix_overlaps_requests(served):
+    ctx, w, m, reqs, res, outs = served
+    spans = sorted((r["admit_s"], r["done_s"]) for r in res)
+    most = max(sum(1 for a, d in spans if a <= t < d) for t, _ in spans)
+    assert most >= 2, spans
+    assert all(r["done_s"] >= r["admit_s"] - 1e-3 for r in res)
+
+
+def test_served_outputs_match_the_oracle(served, oracle):
+    ctx, w, m, reqs, res, outs = served
+    for i in (1, 6):
+        r = reqs[i]
+        o0, o1 = 3 * r["target_begin"], 3 * r["target_end"]
+        lo, hi = m.input_rows(o0, o1)
+        sub = w.model.slice_outputs(o0, o1)
+        for b in range(outs[i].shape[0]):
+            ns = min(1024, r["n_indiv"] - 1024 * b)
+            d = ctx.device_alloc((hi - lo) * 8192)
+            gpu.synth_uniform_device(ctx, gpu.request_block_seed(r["seed"], b), lo, hi - lo, 2048, d.ptr, 8192)
+            ctx.sync()
+            rows = np.zeros((900, 2048), np.int32)
+            rows[lo:hi] = d.download(dtype=np.int32).reshape(hi - lo, 2048)
+            d.free()
+            want, _ = oracle.trlwe_score(sub.term_ptr, sub.term_feat, sub.term_coef, rows, ns, 1, 1024)
+            np.testing.assert_array_equal(outs[i][b], want)
+
+
+def test_requests_beyond_the_budget_are_refused(served):
+    ctx, w, m, reqs, res, outs = served
+    big = dict(arrival_s=0.0, n_indiv=3000, target_begin=0, target_end=1000, seed=1)
+    with pytest.raises(gpu.IdashError) as e:
+        m.serve([big], hbm_budget=64 << 20, max_inflight=2)
+    assert e.value.name == "IDASH_ERR_ADMISSION"
