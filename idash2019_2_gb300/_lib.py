@@ -54,6 +54,11 @@ class LweParams(C.Structure):
     _fields_ = [("n", C.c_uint32), ("n_indiv", C.c_uint32), ("one_t32", C.c_int32)]
 
 
+class IntpolyParams(C.Structure):
+    _fields_ = [("N", C.c_uint32), ("num_samples", C.c_uint32), ("region_size", C.c_uint32),
+                ("one_t32", C.c_int32), ("max_abs_coef", C.c_int32)]
+
+
 class Stats(C.Structure):
     _fields_ = [("kernel_launches", C.c_uint64), ("graph_launches", C.c_uint64),
                 ("h2d_bytes", C.c_uint64), ("d2h_bytes", C.c_uint64)]
@@ -130,6 +135,11 @@ PROTOTYPES = {
     "idash_digest_host": (C.c_uint64, [u32p, C.c_uint64, C.c_uint64]),
     "idash_synth_uniform_device": (status_t, [vp, C.c_uint64, C.c_uint64, C.c_uint64, C.c_uint32, vp, C.c_uint64,
                                               vp]),
+    "idash_model_intpoly": (status_t, [vp, C.POINTER(vp), C.POINTER(IntpolyParams), C.c_uint64, u64p, u32p, i32p,
+                                       C.c_uint64, vp, C.c_int]),
+    "idash_score_intpoly_device": (status_t, [vp, vp, C.POINTER(RowLayout), C.c_uint64, C.c_uint64, vp,
+                                              C.POINTER(RowLayout), vp]),
+    "idash_synth_int16_device": (status_t, [vp, C.c_uint64, C.c_uint64, C.c_int32, vp, vp]),
     "idash_model_get_info": (status_t, [vp, C.POINTER(ModelInfo)]),
     "idash_model_replan": (status_t, [vp]),
     "idash_model_free": (None, [vp]),

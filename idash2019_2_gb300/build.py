@@ -31,6 +31,7 @@ LIB_SOURCES = [
     "csrc/score_kernels.cu",
     "csrc/synth.cu",
     "csrc/noalloc.cu",
+    "csrc/intpoly.cu",
     "csrc/server.cpp",
     "csrc/capi.cpp",
     "csrc/plan.cpp",

@@ -622,6 +622,7 @@ void idash_model_free(idash_model *m) {
         if (m->ctx->stream) cudaStreamSynchronize(m->ctx->stream);
         m->ctx->models.erase(m);
     }
+    m->free_intpoly();
     m->drop_graph();
     m->free_device();
     delete m;

@@ -13,6 +13,7 @@
 #include "score_kernels.cuh"
 
 namespace idash {
+struct IntpolyModel;  // integer-polynomial form (intpoly.cu)
 // Synthetic TRLWE rows [row_begin, row_end) of the generator behind
 // idash_synth_trlwe_device, written to d_out (row row_begin at d_out).
 cudaError_t synth_trlwe_rows(uint64_t seed, const idash_trlwe_params &p, uint64_t n_features, uint64_t row_begin,
@@ -109,6 +110,9 @@ struct idash_model {
     void *g_out = nullptr;
     idash_row_layout g_in_layout{}, g_out_layout{};
 
+    idash::IntpolyModel *intpoly = nullptr;  // set for Form::kIntPoly
+
     void free_device();
     void drop_graph();
+    void free_intpoly();
 };

@@ -10,6 +10,15 @@
 
 namespace idash {
 
+// splitmix64 finaliser (Steele, Lea, Flood 2014): the counter-based mixer of
+// every synthetic generator in the library.
+__host__ __device__ __forceinline__ uint64_t mix64(uint64_t z) {
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
 // ~1 s at the GB300's 2.07 GHz maximum SM clock.
 constexpr long long kWaitLimitCycles = 2000000000ll;
 

@@ -1,0 +1,494 @@
+// Exact integer-polynomial x TRLWE scoring:
+//   out_o = sum_f W_{o,f}(X) * C_f(X)  in Z/2^32[X]/(X^N + 1), on a and b,
+// then b[s] += bias_o * one for s < num_samples and b[j] = 0 for
+// j >= region_size, as the TRLWE form does (eval/idash.cpp:805-810, 839-841).
+// The reference's own terms are the special case W = coef * X^(-r*REGION_SIZE)
+// (eval/idash.cpp:817, 830-833); the only dense polynomial products in the
+// reference are TFHE's double FFT inside encryption and decryption
+// (eval/idash.cpp:625, 714), which cannot be exact here: a term is bounded by
+// N * 2^13 * 2^31 = 2^54 and a 60-term sum by ~2^60, beyond 53 bits.
+//
+// Exactness: every coefficient's true integer value S (ciphertext words taken
+// as signed 32-bit) satisfies |S| <= terms * max|W| * N * 2^31 < p1*p2 / 2,
+// checked when the model is built.  S is computed modulo two NTT primes
+// p1, p2 < 2^31 (p = 1 mod 2N) and recovered by CRT, then reduced mod 2^32.
+//
+// Kernels: k_ntt_model (model polynomials -> Montgomery-form NTT, once per
+// model), k_ntt_rows (input TRLWE rows -> NTT, once per call) and
+// k_intpoly_score (one CTA per output: pointwise multiply-accumulate over the
+// output's terms, inverse NTT, CRT, epilogue).  Negacyclic NTTs are the
+// Cooley-Tukey / Gentleman-Sande pair with bit-reversed powers of a primitive
+// 2N-th root psi (Longa & Naehrig, CANS 2016).
+#include <cstring>
+#include <vector>
+
+#include "capi_internal.hpp"
+#include "common.cuh"
+
+namespace idash {
+
+namespace {
+
+constexpr uint32_t kPrimes[2] = {2147473409u, 2147389441u};  // both = 1 mod 2048
+constexpr uint32_t kPsi2048[2] = {383167813u, 211808905u};   // primitive 2048-th roots of unity
+constexpr int kNttThreads = 256;
+
+struct NttConsts {
+    uint32_t p[2];
+    uint32_t pinv[2];    // -p^-1 mod 2^32
+    uint32_t r2[2];      // R^2 mod p, R = 2^32
+    uint32_t ninv[2];    // N^-1 * R mod p
+    uint32_t p1inv_m;    // p1^-1 * R mod p2
+    uint64_t M, M_half;  // p1 * p2 and floor(M / 2)
+};
+
+uint64_t mulmod(uint64_t a, uint64_t b, uint64_t p) { return uint64_t((unsigned __int128)a * b % p); }
+uint64_t powmod(uint64_t a, uint64_t e, uint64_t p) {
+    uint64_t r = 1;
+    for (a %= p; e; e >>= 1, a = mulmod(a, a, p))
+        if (e & 1) r = mulmod(r, a, p);
+    return r;
+}
+
+__device__ __forceinline__ uint32_t mod_add(uint32_t a, uint32_t b, uint32_t p) {
+    const uint32_t s = a + b;
+    return s >= p ? s - p : s;
+}
+__device__ __forceinline__ uint32_t mod_sub(uint32_t a, uint32_t b, uint32_t p) { return a >= b ? a - b : a + p - b; }
+
+// Montgomery product a*b*2^-32 mod p for a, b < p < 2^31.
+__device__ __forceinline__ uint32_t mont_mul(uint32_t a, uint32_t b, uint32_t p, uint32_t pinv) {
+    const uint64_t t = uint64_t(a) * b;
+    const uint32_t m = uint32_t(t) * pinv;
+    const uint32_t r = uint32_t((t + uint64_t(m) * p) >> 32);
+    return r >= p ? r - p : r;
+}
+
+// A signed 32-bit word (or int16) as a residue mod p.
+__device__ __forceinline__ uint32_t residue(int32_t v, uint32_t p) {
+    int64_t x = int64_t(v) % int64_t(p);
+    return uint32_t(x < 0 ? x + p : x);
+}
+
+// In-place negacyclic NTTs of `narr` arrays of length N in shared memory;
+// array i uses prime prime_of(i) and its twiddles tw[prime][N].
+template <typename PrimeOf>
+__device__ void ntt_forward(uint32_t *arr, int narr, uint32_t N, const uint32_t *tw, const NttConsts &k,
+                            PrimeOf prime_of) {
+    const uint32_t half = N / 2;
+    for (uint32_t m = 1, t = half; m < N; m <<= 1, t >>= 1) {
+        for (uint32_t x = threadIdx.x; x < half * narr; x += blockDim.x) {
+            const uint32_t a = x / half, b = x % half;
+            const uint32_t q = prime_of(a);
+            const uint32_t i = b / t, j = 2 * i * t + b % t;
+            uint32_t *v = arr + a * N;
+            const uint32_t S = tw[q * N + m + i];
+            const uint32_t U = v[j], V = mont_mul(v[j + t], S, k.p[q], k.pinv[q]);
+            v[j] = mod_add(U, V, k.p[q]);
+            v[j + t] = mod_sub(U, V, k.p[q]);
+        }
+        __syncthreads();
+    }
+}
+
+template <typename PrimeOf>
+__device__ void ntt_inverse(uint32_t *arr, int narr, uint32_t N, const uint32_t *itw, const NttConsts &k,
+                            PrimeOf prime_of) {
+    const uint32_t half = N / 2;
+    for (uint32_t h = half, t = 1; h >= 1; h >>= 1, t <<= 1) {
+        for (uint32_t x = threadIdx.x; x < half * narr; x += blockDim.x) {
+            const uint32_t a = x / half, b = x % half;
+            const uint32_t q = prime_of(a);
+            const uint32_t i = b / t, j = 2 * i * t + b % t;
+            uint32_t *v = arr + a * N;
+            const uint32_t S = itw[q * N + h + i];
+            const uint32_t U = v[j], V = v[j + t];
+            v[j] = mod_add(U, V, k.p[q]);
+            v[j + t] = mont_mul(mod_sub(U, V, k.p[q]), S, k.p[q], k.pinv[q]);
+        }
+        __syncthreads();
+    }
+    for (uint32_t x = threadIdx.x; x < N * narr; x += blockDim.x) {
+        const uint32_t q = prime_of(x / N);
+        arr[x] = mont_mul(arr[x], k.ninv[q], k.p[q], k.pinv[q]);
+    }
+    __syncthreads();
+}
+
+// Model polynomials (int16, [term][N]) -> Montgomery-form NTT, [term][prime][N].
+// Coefficients beyond max_abs break the exactness bound: reported, not used.
+__global__ void __launch_bounds__(kNttThreads) k_ntt_model(const int16_t *w, uint64_t n_terms, uint32_t N,
+                                                           const uint32_t *tw, NttConsts k, int32_t max_abs,
+                                                           uint32_t *w_hat, uint32_t *err) {
+    extern __shared__ uint32_t sh[];
+    uint32_t *tws = sh;           // 2 * N forward twiddles
+    uint32_t *arr = sh + 2 * N;   // 2 arrays (one per prime)
+    for (uint32_t x = threadIdx.x; x < 2 * N; x += blockDim.x) tws[x] = tw[x];
+    __syncthreads();
+    for (uint64_t t = blockIdx.x; t < n_terms; t += gridDim.x) {
+        const int16_t *src = w + t * N;
+        for (uint32_t x = threadIdx.x; x < N; x += blockDim.x) {
+            const int32_t v = src[x];
+            if (v > max_abs || v < -max_abs) report_error(err, kDevBadIndex);
+            arr[x] = residue(v, k.p[0]);
+            arr[N + x] = residue(v, k.p[1]);
+        }
+        __syncthreads();
+        ntt_forward(arr, 2, N, tws, k, [](uint32_t a) { return a; });
+        uint32_t *dst = w_hat + t * 2 * N;
+        for (uint32_t x = threadIdx.x; x < 2 * N; x += blockDim.x) {
+            const uint32_t q = x / N;
+            dst[x] = mont_mul(arr[x], k.r2[q], k.p[q], k.pinv[q]);
+        }
+        __syncthreads();
+    }
+}
+
+// Input TRLWE rows (a | b, signed words) -> NTT, [row][poly][prime][N].
+__global__ void __launch_bounds__(kNttThreads) k_ntt_rows(const uint8_t *in, uint64_t stride, uint64_t n_rows,
+                                                          uint32_t N, const uint32_t *tw, NttConsts k,
+                                                          uint32_t *c_hat) {
+    extern __shared__ uint32_t sh[];
+    uint32_t *tws = sh;          // 2 * N
+    uint32_t *arr = sh + 2 * N;  // 4 arrays: (a,p1) (a,p2) (b,p1) (b,p2)
+    for (uint32_t x = threadIdx.x; x < 2 * N; x += blockDim.x) tws[x] = tw[x];
+    __syncthreads();
+    for (uint64_t r = blockIdx.x; r < n_rows; r += gridDim.x) {
+        const int32_t *src = reinterpret_cast<const int32_t *>(in + r * stride);
+        for (uint32_t x = threadIdx.x; x < 2 * N; x += blockDim.x) {
+            const uint32_t poly = x / N, j = x % N;
+            const int32_t v = src[x];
+            arr[(2 * poly) * N + j] = residue(v, k.p[0]);
+            arr[(2 * poly + 1) * N + j] = residue(v, k.p[1]);
+        }
+        __syncthreads();
+        ntt_forward(arr, 4, N, tws, k, [](uint32_t a) { return a & 1u; });
+        uint4 *dst = reinterpret_cast<uint4 *>(c_hat + r * 4 * N);
+        const uint4 *s4 = reinterpret_cast<const uint4 *>(arr);
+        for (uint32_t x = threadIdx.x; x < N; x += blockDim.x) dst[x] = s4[x];
+        __syncthreads();
+    }
+}
+
+struct IntpolyArgs {
+    const uint64_t *term_ptr;
+    const uint32_t *term_row;
+    const uint32_t *w_hat;
+    const uint32_t *c_hat;
+    const int32_t *bias;
+    const uint32_t *itw;
+    NttConsts k;
+    uint32_t N, num_samples, region_size, n_rows;
+    int32_t one;
+    uint64_t out_begin, out_end;
+    uint8_t *out;  // payload of output row 0 (output o -> row o - out_begin)
+    uint64_t out_stride;
+    uint32_t *err;
+};
+
+// One CTA per output; thread x owns NTT points 4x..4x+3 of the four arrays.
+__global__ void __launch_bounds__(kNttThreads) k_intpoly_score(const IntpolyArgs a) {
+    extern __shared__ uint32_t sh[];
+    uint32_t *itws = sh;         // 2 * N inverse twiddles
+    uint32_t *arr = sh + 2 * a.N;  // 4 arrays
+    const uint32_t N = a.N;
+    for (uint32_t x = threadIdx.x; x < 2 * N; x += blockDim.x) itws[x] = a.itw[x];
+    const uint32_t p0 = a.k.p[0], p1 = a.k.p[1], i0 = a.k.pinv[0], i1 = a.k.pinv[1];
+    for (uint64_t o = a.out_begin + blockIdx.x; o < a.out_end; o += gridDim.x) {
+        uint32_t acc[16];  // [poly*2 + prime][4]
+#pragma unroll
+        for (int e = 0; e < 16; ++e) acc[e] = 0;
+        for (uint64_t t = a.term_ptr[o]; t < a.term_ptr[o + 1]; ++t) {
+            const uint32_t r = a.term_row[t];
+            if (r >= a.n_rows) {
+                report_error(a.err, kDevBadIndex);
+                continue;
+            }
+            const uint4 *wv = reinterpret_cast<const uint4 *>(a.w_hat + t * 2 * N);
+            const uint4 *cv = reinterpret_cast<const uint4 *>(a.c_hat + uint64_t(r) * 4 * N);
+            const uint4 w0 = wv[threadIdx.x], w1 = wv[N / 4 + threadIdx.x];
+            const uint32_t W[2][4] = {{w0.x, w0.y, w0.z, w0.w}, {w1.x, w1.y, w1.z, w1.w}};
+#pragma unroll
+            for (int ap = 0; ap < 4; ++ap) {  // (poly, prime)
+                const uint4 c = cv[ap * (N / 4) + threadIdx.x];
+                const uint32_t Cv[4] = {c.x, c.y, c.z, c.w};
+                const int q = ap & 1;
+                const uint32_t p = q ? p1 : p0, pinv = q ? i1 : i0;
+#pragma unroll
+                for (int e = 0; e < 4; ++e) acc[ap * 4 + e] = mod_add(acc[ap * 4 + e], mont_mul(W[q][e], Cv[e], p, pinv), p);
+            }
+        }
+        __syncthreads();  // previous output's readers of arr are done
+#pragma unroll
+        for (int ap = 0; ap < 4; ++ap)
+#pragma unroll
+            for (int e = 0; e < 4; ++e) arr[ap * N + 4 * threadIdx.x + e] = acc[ap * 4 + e];
+        __syncthreads();
+        ntt_inverse(arr, 4, N, itws, a.k, [](uint32_t x) { return x & 1u; });
+        // CRT: x = x1 + p1 * ((x2 - x1) / p1 mod p2), signed, then mod 2^32
+        uint32_t *dst = reinterpret_cast<uint32_t *>(a.out + (o - a.out_begin) * a.out_stride);
+        const uint32_t bias = uint32_t(a.bias ? a.bias[o] : 0) * uint32_t(a.one);
+        for (uint32_t x = threadIdx.x; x < 2 * N; x += blockDim.x) {
+            const uint32_t poly = x / N, j = x % N;
+            const uint32_t x1 = arr[(2 * poly) * N + j], x2 = arr[(2 * poly + 1) * N + j];
+            const uint32_t x1m = x1 >= p1 ? x1 - p1 : x1;
+            const uint32_t t = mont_mul(mod_sub(x2, x1m, p1), a.k.p1inv_m, p1, i1);
+            uint64_t v = uint64_t(x1) + uint64_t(p0) * t;
+            uint32_t w = uint32_t(v);
+            if (v > a.k.M_half) w -= uint32_t(a.k.M);
+            if (poly == 1) {
+                if (j < a.num_samples) w += bias;
+                if (j >= a.region_size) w = 0;
+            }
+            dst[x] = w;
+        }
+    }
+}
+
+__global__ void k_synth_int16(uint64_t seed, uint64_t n, int32_t max_abs, int16_t *out) {
+    const uint64_t key = mix64(seed + mix64(15));
+    const uint32_t span = uint32_t(2 * max_abs);
+    for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += uint64_t(gridDim.x) * blockDim.x)
+        out[i] = int16_t(int32_t(uint32_t(mix64(key ^ i) >> 32) % span) - max_abs);
+}
+
+NttConsts make_consts(uint32_t N) {
+    NttConsts k{};
+    for (int q = 0; q < 2; ++q) {
+        const uint64_t p = kPrimes[q];
+        k.p[q] = uint32_t(p);
+        uint32_t inv = 1;  // Newton iteration for p^-1 mod 2^32
+        for (int it = 0; it < 5; ++it) inv *= 2u - uint32_t(p) * inv;
+        k.pinv[q] = 0u - inv;
+        const uint64_t R = (uint64_t(1) << 32) % p;
+        k.r2[q] = uint32_t(mulmod(R, R, p));
+        k.ninv[q] = uint32_t(mulmod(powmod(N, p - 2, p), R, p));
+    }
+    const uint64_t p0 = kPrimes[0], p1 = kPrimes[1];
+    k.p1inv_m = uint32_t(mulmod(powmod(p0 % p1, p1 - 2, p1), (uint64_t(1) << 32) % p1, p1));
+    k.M = p0 * p1;
+    k.M_half = k.M / 2;
+    return k;
+}
+
+// Bit-reversed powers of psi (forward) and psi^-1 (inverse), Montgomery form,
+// [prime][N] each.  psi is a primitive 2N-th root: psi_2048^(2048 / 2N).
+void make_twiddles(uint32_t N, std::vector<uint32_t> *fwd, std::vector<uint32_t> *inv) {
+    uint32_t logn = 0;
+    while ((1u << logn) < N) ++logn;
+    fwd->assign(2 * N, 0);
+    inv->assign(2 * N, 0);
+    for (int q = 0; q < 2; ++q) {
+        const uint64_t p = kPrimes[q];
+        const uint64_t psi = powmod(kPsi2048[q], 2048 / (2 * N), p);
+        const uint64_t psi_inv = powmod(psi, p - 2, p);
+        const uint64_t R = (uint64_t(1) << 32) % p;
+        for (uint32_t i = 0; i < N; ++i) {
+            uint32_t rev = 0;
+            for (uint32_t b = 0; b < logn; ++b)
+                if (i & (1u << b)) rev |= 1u << (logn - 1 - b);
+            (*fwd)[q * N + i] = uint32_t(mulmod(powmod(psi, rev, p), R, p));
+            (*inv)[q * N + i] = uint32_t(mulmod(powmod(psi_inv, rev, p), R, p));
+        }
+    }
+}
+
+}  // namespace
+
+struct IntpolyModel {
+    uint32_t N = 0, num_samples = 0, region_size = 0;
+    int32_t one = 0;
+    uint64_t n_out = 0, n_terms = 0, n_rows = 0;
+    NttConsts k{};
+    uint64_t *d_term_ptr = nullptr;
+    uint32_t *d_term_row = nullptr;
+    int32_t *d_bias = nullptr;
+    uint32_t *d_w_hat = nullptr;
+    uint32_t *d_tw = nullptr;   // forward twiddles [2][N]
+    uint32_t *d_itw = nullptr;  // inverse twiddles [2][N]
+    uint32_t *d_c_hat = nullptr;
+    uint64_t c_hat_rows = 0;
+    ~IntpolyModel() {
+        cudaFree(d_term_ptr);
+        cudaFree(d_term_row);
+        cudaFree(d_bias);
+        cudaFree(d_w_hat);
+        cudaFree(d_tw);
+        cudaFree(d_itw);
+        cudaFree(d_c_hat);
+    }
+};
+
+}  // namespace idash
+
+using namespace idash;
+
+void idash_model::free_intpoly() {
+    delete intpoly;
+    intpoly = nullptr;
+}
+
+extern "C" idash_status idash_model_intpoly(idash_ctx *ctx, idash_model **model, const idash_intpoly_params *p,
+                                            uint64_t n_out, const uint64_t *term_ptr, const uint32_t *term_feat,
+                                            const int32_t *bias, uint64_t n_in_rows, const int16_t *term_poly,
+                                            int term_poly_on_device) {
+    if (!ctx || !model || !p || (n_out && !term_ptr)) return IDASH_ERR_INVALID_ARGUMENT;
+    *model = nullptr;
+    if (p->N != 4 * kNttThreads)
+        return ctx->fail(IDASH_ERR_UNSUPPORTED, "the integer-polynomial kernels are built for N = 1024");
+    if (p->num_samples > p->region_size || p->region_size > p->N)
+        return ctx->fail(IDASH_ERR_INVALID_ARGUMENT, "need num_samples <= region_size <= N");
+    if (p->max_abs_coef <= 0 || p->max_abs_coef > 32767)
+        return ctx->fail(IDASH_ERR_INVALID_ARGUMENT, "max_abs_coef must be in [1, 32767]");
+    const uint64_t nnz = n_out ? term_ptr[n_out] : 0;
+    if (nnz && (!term_feat || !term_poly)) return IDASH_ERR_INVALID_ARGUMENT;
+    const NttConsts k = make_consts(p->N);
+    // exactness: terms * max|W| * N * 2^31 < M / 2 for every output
+    const double cap = double(k.M_half) / (double(p->max_abs_coef) * p->N * 2147483648.0);
+    for (uint64_t o = 0; o < n_out; ++o) {
+        if (term_ptr[o + 1] < term_ptr[o]) return ctx->fail(IDASH_ERR_INVALID_ARGUMENT, "term_ptr not monotone");
+        if (double(term_ptr[o + 1] - term_ptr[o]) >= cap)
+            return ctx->fail(IDASH_ERR_UNSUPPORTED, "output " + std::to_string(o) + " has too many terms for an "
+                                                    "exact two-prime product at this max_abs_coef");
+    }
+    for (uint64_t t = 0; t < nnz; ++t)
+        if (term_feat[t] >= n_in_rows) return ctx->fail(IDASH_ERR_INDEX, "a term names a row outside the input");
+
+    idash_model *m = new idash_model();
+    m->ctx = ctx;
+    m->form = Form::kIntPoly;
+    m->n_out = n_out;
+    m->n_in_rows = n_in_rows;
+    m->intpoly = new IntpolyModel();
+    IntpolyModel &ip = *m->intpoly;
+    ip.N = p->N;
+    ip.num_samples = p->num_samples;
+    ip.region_size = p->region_size;
+    ip.one = p->one_t32;
+    ip.n_out = n_out;
+    ip.n_terms = nnz;
+    ip.n_rows = n_in_rows;
+    ip.k = k;
+    std::vector<uint32_t> fwd, inv;
+    make_twiddles(p->N, &fwd, &inv);
+    std::vector<int32_t> bias_v(n_out, 0);
+    if (bias) std::memcpy(bias_v.data(), bias, n_out * 4);
+    auto fail = [&](idash_status s) {
+        idash_model_free(m);
+        return s;
+    };
+    idash_status s = IDASH_OK;
+    auto up = [&](void **dst, const void *src, size_t bytes, const char *what) {
+        if (s != IDASH_OK) return;
+        s = ctx->check_cuda(cudaMalloc(dst, std::max<size_t>(bytes, 16)), what);
+        if (s == IDASH_OK && bytes) s = ctx->check_cuda(cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice), what);
+    };
+    up(reinterpret_cast<void **>(&ip.d_term_ptr), term_ptr, (n_out + 1) * 8, "intpoly term_ptr");
+    up(reinterpret_cast<void **>(&ip.d_term_row), term_feat, nnz * 4, "intpoly term rows");
+    up(reinterpret_cast<void **>(&ip.d_bias), bias_v.data(), n_out * 4, "intpoly bias");
+    up(reinterpret_cast<void **>(&ip.d_tw), fwd.data(), fwd.size() * 4, "intpoly twiddles");
+    up(reinterpret_cast<void **>(&ip.d_itw), inv.data(), inv.size() * 4, "intpoly twiddles");
+    if (s == IDASH_OK)
+        s = ctx->check_cuda(cudaMalloc(&ip.d_w_hat, std::max<size_t>(nnz * 2 * p->N * 4, 16)), "cudaMalloc(W^)");
+    if (s != IDASH_OK) return fail(s);
+    // Model polynomials -> NTT, through a bounded device staging buffer when on the host.
+    const size_t smem = size_t(4) * p->N * 4;
+    const uint64_t chunk = term_poly_on_device ? nnz : std::min<uint64_t>(nnz, (uint64_t(1) << 28) / p->N);
+    int16_t *stage = nullptr;
+    if (!term_poly_on_device && nnz &&
+        (s = ctx->check_cuda(cudaMalloc(&stage, chunk * p->N * 2), "cudaMalloc(model staging)")) != IDASH_OK)
+        return fail(s);
+    for (uint64_t t0 = 0; t0 < nnz && s == IDASH_OK; t0 += chunk) {
+        const uint64_t n = std::min(chunk, nnz - t0);
+        const int16_t *src = term_poly + t0 * p->N;
+        if (!term_poly_on_device) {
+            s = ctx->check_cuda(cudaMemcpy(stage, src, n * p->N * 2, cudaMemcpyHostToDevice), "model upload");
+            src = stage;
+        }
+        if (s != IDASH_OK) break;
+        const uint32_t grid = uint32_t(std::min<uint64_t>(n, uint64_t(ctx->sm_count) * 8));
+        k_ntt_model<<<grid, kNttThreads, smem, ctx->stream>>>(src, n, p->N, ip.d_tw, k, p->max_abs_coef,
+                                                             ip.d_w_hat + t0 * 2 * p->N, ctx->d_err);
+        s = ctx->check_cuda(cudaGetLastError(), "k_ntt_model launch");
+        if (s == IDASH_OK) s = idash_sync(ctx);
+    }
+    cudaFree(stage);
+    if (s != IDASH_OK) {
+        if (s == IDASH_ERR_INDEX) ctx->last_error = "a model coefficient exceeds max_abs_coef";
+        return fail(s);
+    }
+    ctx->models.insert(m);
+    *model = m;
+    return IDASH_OK;
+}
+
+extern "C" idash_status idash_score_intpoly_device(idash_model *m, const void *d_in, const idash_row_layout *il,
+                                                   uint64_t out_begin, uint64_t out_end, void *d_out,
+                                                   const idash_row_layout *ol, void *stream) {
+    if (!m || !d_in || !d_out || !il || !ol) return IDASH_ERR_INVALID_ARGUMENT;
+    idash_ctx *ctx = m->ctx;
+    if (m->form != Form::kIntPoly || !m->intpoly) return ctx->fail(IDASH_ERR_STATE, "not an integer-polynomial model");
+    IntpolyModel &ip = *m->intpoly;
+    if (out_begin > out_end || out_end > ip.n_out) return ctx->fail(IDASH_ERR_INVALID_ARGUMENT, "bad output range");
+    const uint64_t payload = uint64_t(2) * ip.N * 4;
+    if (il->row_stride % 16 || ol->row_stride % 16 || il->payload_offset + payload > il->row_stride ||
+        ol->payload_offset + payload > ol->row_stride ||
+        ((reinterpret_cast<uintptr_t>(d_in) + il->payload_offset) & 15u) ||
+        ((reinterpret_cast<uintptr_t>(d_out) + ol->payload_offset) & 15u))
+        return ctx->fail(IDASH_ERR_INVALID_ARGUMENT, "row layout: stride or alignment");
+    if (out_begin == out_end) return IDASH_OK;
+    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+    idash_status s = IDASH_OK;
+    if (ip.c_hat_rows < ip.n_rows) {
+        cudaStreamSynchronize(st);
+        cudaFree(ip.d_c_hat);
+        ip.d_c_hat = nullptr;
+        ip.c_hat_rows = 0;
+        if ((s = ctx->check_cuda(cudaMalloc(&ip.d_c_hat, std::max<uint64_t>(ip.n_rows, 1) * 4 * ip.N * 4),
+                                 "cudaMalloc(C^)")) != IDASH_OK)
+            return s;
+        ip.c_hat_rows = ip.n_rows;
+    }
+    const size_t smem_rows = size_t(6) * ip.N * 4;
+    const uint32_t grid_rows = uint32_t(std::min<uint64_t>(ip.n_rows, uint64_t(ctx->sm_count) * 8));
+    if (grid_rows) {
+        k_ntt_rows<<<grid_rows, kNttThreads, smem_rows, st>>>(static_cast<const uint8_t *>(d_in) + il->payload_offset,
+                                                             il->row_stride, ip.n_rows, ip.N, ip.d_tw, ip.k,
+                                                             ip.d_c_hat);
+        if ((s = ctx->check_cuda(cudaGetLastError(), "k_ntt_rows launch")) != IDASH_OK) return s;
+    }
+    IntpolyArgs a{};
+    a.term_ptr = ip.d_term_ptr;
+    a.term_row = ip.d_term_row;
+    a.w_hat = ip.d_w_hat;
+    a.c_hat = ip.d_c_hat;
+    a.bias = ip.d_bias;
+    a.itw = ip.d_itw;
+    a.k = ip.k;
+    a.N = ip.N;
+    a.num_samples = ip.num_samples;
+    a.region_size = ip.region_size;
+    a.n_rows = uint32_t(ip.n_rows);
+    a.one = ip.one;
+    a.out_begin = out_begin;
+    a.out_end = out_end;
+    a.out = static_cast<uint8_t *>(d_out) + ol->payload_offset;
+    a.out_stride = ol->row_stride;
+    a.err = ctx->d_err;
+    const size_t smem = size_t(6) * ip.N * 4;
+    const uint32_t grid = uint32_t(std::min<uint64_t>(out_end - out_begin, uint64_t(ctx->sm_count) * 8));
+    k_intpoly_score<<<grid, kNttThreads, smem, st>>>(a);
+    s = ctx->check_cuda(cudaGetLastError(), "k_intpoly_score launch");
+    if (s == IDASH_OK) ctx->stats.kernel_launches += 2;
+    return s;
+}
+
+extern "C" idash_status idash_synth_int16_device(idash_ctx *ctx, uint64_t seed, uint64_t n, int32_t max_abs,
+                                                 int16_t *d_out, void *stream) {
+    if (!ctx || !d_out || max_abs <= 0 || max_abs > 16383) return IDASH_ERR_INVALID_ARGUMENT;
+    if (n == 0) return IDASH_OK;
+    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+    const uint32_t grid = uint32_t(std::min<uint64_t>((n + 255) / 256, uint64_t(ctx->sm_count) * 16));
+    k_synth_int16<<<grid, 256, 0, st>>>(seed, n, max_abs, d_out);
+    return ctx->check_cuda(cudaGetLastError(), "k_synth_int16 launch");
+}

@@ -53,7 +53,7 @@ struct PlanTerm {
 constexpr uint32_t kNoOutput = 0xFFFFFFFFu;
 constexpr uint32_t kConstantFeature = 0xFFFFFFFFu;
 
-enum class Form : int { kTrlwe = 0, kLwe = 1 };
+enum class Form : int { kTrlwe = 0, kLwe = 1, kIntPoly = 2 };
 
 struct PlanInput {
     Form form = Form::kTrlwe;

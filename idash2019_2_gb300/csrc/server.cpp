@@ -99,22 +99,10 @@ extern "C" idash_status idash_serve_trlwe(idash_model *m, const idash_serve_conf
     const uint64_t row_bytes = uint64_t(2) * N * 4;
     const idash_row_layout dense{row_bytes, 0, -1, -1};
 
-    // Shapes and admission limits first: a request that can never fit fails
-    // with IDASH_ERR_ADMISSION before anything runs.
-    std::vector<Shape> shape(n);
     for (uint64_t i = 0; i < n; ++i) {
         const idash_request &r = reqs[i];
-        Shape &s = shape[i];
         if (r.n_indiv == 0 || r.target_end <= r.target_begin || 3 * r.target_end > m->n_out)
             return ctx->fail(IDASH_ERR_INVALID_ARGUMENT, "request " + std::to_string(i) + ": empty or out of range");
-        s.out_begin = 3 * r.target_begin;
-        s.out_end = 3 * r.target_end;
-        idash_model_input_rows(m, s.out_begin, s.out_end, &s.row_begin, &s.row_end);
-        s.blocks = (r.n_indiv + RS - 1) / RS;
-        s.in_bytes_per_block = std::max<uint64_t>(s.row_end - s.row_begin, 1) * row_bytes;
-        s.out_bytes_per_block = (s.out_end - s.out_begin) * row_bytes;
-        if (s.bytes() > cfg->hbm_budget)
-            return ctx->fail(IDASH_ERR_ADMISSION, "request " + std::to_string(i) + " needs more than the HBM budget");
     }
 
     uint8_t *arena_base = nullptr;
@@ -139,6 +127,23 @@ extern "C" idash_status idash_serve_trlwe(idash_model *m, const idash_serve_conf
             st = idash_score_trlwe_device(m, arena_base, &dense, arena_base + in_b, &dense, nullptr);
             if (st == IDASH_OK) st = idash_sync(ctx);
         }
+    }
+
+    // Shapes under the final plan (blocks decide which input rows a range
+    // reads) and admission limits: a request that can never fit fails with
+    // IDASH_ERR_ADMISSION before any request runs.
+    std::vector<Shape> shape(n);
+    for (uint64_t i = 0; i < n && st == IDASH_OK; ++i) {
+        const idash_request &r = reqs[i];
+        Shape &s = shape[i];
+        s.out_begin = 3 * r.target_begin;
+        s.out_end = 3 * r.target_end;
+        idash_model_input_rows(m, s.out_begin, s.out_end, &s.row_begin, &s.row_end);
+        s.blocks = (r.n_indiv + RS - 1) / RS;
+        s.in_bytes_per_block = std::max<uint64_t>(s.row_end - s.row_begin, 1) * row_bytes;
+        s.out_bytes_per_block = (s.out_end - s.out_begin) * row_bytes;
+        if (s.bytes() > cfg->hbm_budget)
+            st = ctx->fail(IDASH_ERR_ADMISSION, "request " + std::to_string(i) + " needs more than the HBM budget");
     }
 
     Arena arena(cfg->hbm_budget);

@@ -26,13 +26,6 @@
 
 namespace idash {
 
-__host__ __device__ __forceinline__ uint64_t mix64(uint64_t z) {
-    z += 0x9E3779B97F4A7C15ull;
-    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
-    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
-    return z ^ (z >> 31);
-}
-
 __host__ __device__ __forceinline__ uint64_t stream_key(uint64_t seed, uint64_t stream) {
     return mix64(seed + mix64(stream));
 }

@@ -345,6 +345,52 @@ class LweModel:
             out_stride_words, C.c_void_p(stream) if stream else None))
 
 
+class IntpolyModel:
+    """A resident integer-polynomial x TRLWE model (idash_model_intpoly)."""
+
+    def __init__(self, ctx: Context, csr: CSRModel, term_poly, n_in_rows: int, num_samples: int,
+                 region_size: int, bias=None, N: int = N_DEFAULT, one_t32: int = ONE_IN_T32,
+                 max_abs_coef: int = 8192, poly_on_device: bool = False):
+        self.ctx, self.csr, self.N = ctx, csr, N
+        self.params = _lib.IntpolyParams(N, num_samples, region_size, one_t32, max_abs_coef)
+        keep = [np.ascontiguousarray(csr.term_ptr, np.uint64), np.ascontiguousarray(csr.term_feat, np.uint32)]
+        b = None if bias is None else np.ascontiguousarray(bias, np.int32)
+        if poly_on_device:
+            poly_ptr = C.c_void_p(term_poly)
+        else:
+            tp = np.ascontiguousarray(term_poly, np.int16)
+            keep.append(tp)
+            poly_ptr = tp.ctypes.data_as(C.c_void_p)
+        h = C.c_void_p()
+        ctx.check(ctx.lib.idash_model_intpoly(ctx.h, C.byref(h), C.byref(self.params), csr.n_out,
+                                              _p(keep[0], C.c_uint64), _p(keep[1], C.c_uint32), _p(b, C.c_int32),
+                                              n_in_rows, poly_ptr, 1 if poly_on_device else 0))
+        self.h = h
+        self.n_out = csr.n_out
+        ctx._own(self)
+
+    def free(self):
+        if self.h and self.ctx.h:
+            self.ctx.lib.idash_model_free(self.h)
+        self.h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+    def score_device(self, d_in: int, in_layout: RowLayout, out_begin: int, out_end: int, d_out: int,
+                     out_layout: RowLayout, stream=None):
+        self.ctx.check(self.ctx.lib.idash_score_intpoly_device(
+            self.h, C.c_void_p(d_in), C.byref(in_layout), out_begin, out_end, C.c_void_p(d_out), C.byref(out_layout),
+            C.c_void_p(stream) if stream else None))
+
+
+def synth_int16_device(ctx: Context, seed: int, n: int, max_abs: int, d_out: int):
+    ctx.check(ctx.lib.idash_synth_int16_device(ctx.h, seed, n, max_abs, C.c_void_p(d_out), None))
+
+
 def lwe_row_words(n_indiv: int, n: int = 1024) -> int:
     """Row stride (int32 words) of a per-individual LWE row: n_indiv*(n+1) rounded to 4."""
     return (n_indiv * (n + 1) + 3) // 4 * 4

@@ -225,6 +225,38 @@ idash_status idash_score_lwe_device(idash_model *model, uint32_t n_indiv, const 
                                     uint64_t in_row_stride, uint64_t out_begin, uint64_t out_end,
                                     int32_t *d_out, uint64_t out_row_stride, void *stream);
 
+/* ------------------------------------------- integer-polynomial x TRLWE
+ * The generalisation of the TRLWE form to dense integer-polynomial weights:
+ * out_o = sum_f W_{o,f}(X) * C_f(X) mod (X^N + 1, 2^32) on both polynomials,
+ * then b[s] += bias_o * one_t32 for s < num_samples, b[j] = 0 for
+ * j >= region_size.  The reference's terms are W = coef * X^(-r*REGION_SIZE)
+ * (eval/idash.cpp:817, 830-833).  Exact: two-prime NTT + CRT, no floating
+ * point.  Terms per output must satisfy terms * max_abs_coef * N * 2^31 <
+ * p1*p2/2 (about 127 terms at |W| <= 8192); checked at model creation. */
+typedef struct {
+    uint32_t N;            /* 1024 */
+    uint32_t num_samples;  /* b slots that receive the bias */
+    uint32_t region_size;  /* b[j] = 0 for j >= region_size (N: none) */
+    int32_t one_t32;       /* bias scaling (2^18) */
+    int32_t max_abs_coef;  /* bound on |W| coefficients (8192) */
+} idash_intpoly_params;
+/* term_poly: [nnz][N] int16 weight polynomials (host, or device when
+ * term_poly_on_device); term_feat: the input TRLWE row of each term; bias:
+ * one integer per output (NULL: 0).  The weights are transformed once and
+ * kept resident (nnz * 8 KiB of HBM at N = 1024). */
+idash_status idash_model_intpoly(idash_ctx *ctx, idash_model **model, const idash_intpoly_params *params,
+                                 uint64_t n_out, const uint64_t *term_ptr, const uint32_t *term_feat,
+                                 const int32_t *bias, uint64_t n_in_rows, const int16_t *term_poly,
+                                 int term_poly_on_device);
+/* Scores outputs [out_begin, out_end) (output o -> row o - out_begin) from
+ * the n_in_rows input TRLWE rows at d_in.  Asynchronous on `stream`. */
+idash_status idash_score_intpoly_device(idash_model *model, const void *d_in, const idash_row_layout *in_layout,
+                                        uint64_t out_begin, uint64_t out_end, void *d_out,
+                                        const idash_row_layout *out_layout, void *stream);
+/* Seeded int16 weights uniform in [-max_abs, max_abs) on the device. */
+idash_status idash_synth_int16_device(idash_ctx *ctx, uint64_t seed, uint64_t n, int32_t max_abs, int16_t *d_out,
+                                      void *stream);
+
 /* Model facts: outputs, total terms, planned blocks, slice width chosen. */
 typedef struct {
     uint64_t n_out, n_terms, n_groups, n_blocks, n_slots;

@@ -98,6 +98,24 @@ def lwe_score(term_ptr, term_feat, term_coef, rows, n_indiv, out_begin, out_end,
     return out
 
 
+def intpoly_score(term_ptr, term_feat, term_poly, bias, rows, num_samples, region_size, out_begin, out_end,
+                  one_t32=ONE_IN_T32, n_threads=0):
+    """Oracle B, integer-polynomial form (exact schoolbook negacyclic product)."""
+    tp = np.ascontiguousarray(term_ptr, np.uint64)
+    tf = np.ascontiguousarray(term_feat, np.uint32)
+    tw = np.ascontiguousarray(term_poly, np.int16)
+    b = np.ascontiguousarray(bias, np.int32)
+    rows = np.ascontiguousarray(rows, np.int32)
+    N = rows.shape[1] // 2
+    out = np.zeros((out_end - out_begin, 2 * N), np.int32)
+    rc = lib().oracle_intpoly_score(N, num_samples, region_size, one_t32, len(tp) - 1, _p(tp, C.c_uint64),
+                                    _p(tf, C.c_uint32), _p(tw, C.c_int16), _p(b, C.c_int32), rows.shape[0],
+                                    _p(rows, C.c_int32), out_begin, out_end, _p(out, C.c_int32), n_threads)
+    if rc != 0:
+        raise ValueError(f"oracle_intpoly_score failed ({rc})")
+    return out
+
+
 def sample_extract(trlwe_row: np.ndarray, slot: int) -> np.ndarray:
     row = np.ascontiguousarray(trlwe_row, np.int32)
     out = np.zeros(len(row) // 2 + 1, np.int32)
