@@ -265,6 +265,57 @@ def section_lwe(ctx, name, seed, n_indiv, n_tags, n_targets, neighbours=5, choic
     return out
 
 
+def section_intpoly(ctx, seed, passes=5):
+    """Integer-polynomial x TRLWE product at full scale: 48,552 input TRLWE
+    (16,184 tags x 3), 242,646 outputs (80,882 targets x 3), 20 neighbours
+    (60 dense int16 weight polynomials per output, |w| <= 8192), one block of
+    1,024 individuals per TRLWE.  Exact (two-prime NTT + CRT)."""
+    import numpy as np
+    from idash2019_2_gb300 import gpu
+    w = gpu.synth_model(seed, 16184, 80882, neighbours=20)
+    csr = w.model
+    const = csr.term_feat == 0xFFFFFFFF
+    counts = np.diff(csr.term_ptr.astype(np.int64)) - np.add.reduceat(const.astype(np.int64),
+                                                                        csr.term_ptr[:-1].astype(np.int64))
+    ptr = np.concatenate([[0], np.cumsum(counts)]).astype(np.uint64)
+    feat = csr.term_feat[~const]
+    bias = np.zeros(csr.n_out, np.int32)
+    owner = np.repeat(np.arange(csr.n_out), np.diff(csr.term_ptr.astype(np.int64)))
+    bias[owner[const]] = csr.term_coef[const]
+    icsr = gpu.CSRModel(ptr, feat, np.zeros(len(feat), np.int32))
+    n_terms, n_rows = len(feat), 3 * 16184
+    d_poly = ctx.device_alloc(n_terms * 1024 * 2)
+    gpu.synth_int16_device(ctx, seed, n_terms * 1024, 8192, d_poly.ptr)
+    t0 = time.perf_counter()
+    m = gpu.IntpolyModel(ctx, icsr, d_poly.ptr, n_rows, 1024, 1024, bias=bias, poly_on_device=True)
+    build_s = time.perf_counter() - t0
+    d_poly.free()
+    params = gpu.TrlweParams(1024, 1, 1024, 1, 1024, 1 << 18, 42)
+    d_in = ctx.device_alloc(n_rows * 8192)
+    gpu.synth_trlwe_device(ctx, seed, params, 16184, d_in.ptr, gpu.DENSE_TRLWE)
+    d_out = ctx.device_alloc(csr.n_out * 8192)
+    run = lambda: m.score_device(d_in.ptr, gpu.DENSE_TRLWE, 0, csr.n_out, d_out.ptr, gpu.DENSE_TRLWE)
+    run()
+    ms = time_on_stream(ctx, run, passes)
+    # compulsory traffic of this algorithm per pass: the NTT-domain weights
+    # (2 primes x N words per term), input rows in and their NTT out and back
+    # in, output rows out
+    traffic = n_terms * 2 * 1024 * 4 + n_rows * 8192 + 2 * n_rows * 4 * 1024 * 4 + csr.n_out * 8192
+    peak, _ = peaks()
+    out = {"value": csr.n_out * 1024 / (ms / 1e3), "unit": UNIT, "ms_per_step": ms,
+           "outputs_per_s": csr.n_out / (ms / 1e3), "terms": n_terms, "model_build_s": build_s,
+           "schoolbook_mac_per_s": n_terms * 2 * 1024 * 1024 / (ms / 1e3),
+           "resident_weight_bytes": n_terms * 2 * 1024 * 4,
+           "roofline": {"bound": "hbm", "achieved": traffic / (ms / 1e3) / 1e9, "peak": peak, "unit": "GB/s",
+                        "frac": traffic / (ms / 1e3) / 1e9 / peak, "algorithmic_bytes_per_step": traffic},
+           "workload": "integer-polynomial x TRLWE: 48,552 input TRLWE, 242,646 outputs, 60 dense int16 weight "
+                       "polynomials per output, N=1024, 1,024 individuals per TRLWE (predictions = outputs x 1024)"}
+    for b in (d_in, d_out):
+        b.free()
+    m.free()
+    return out
+
+
 def section_serving(ctx, seed, n_requests=10000, budget=150 << 30, inflight=4):
     """Continuous batching (idash_serve_trlwe) over a Poisson stream: each
     request has individuals ~ U[1, 2000] and a contiguous target range of
@@ -425,6 +476,8 @@ def run_ours(args):
                                                    "individuals x 80,882 targets x 3, neighbours uniform from "
                                                    "{5,10,20,30,50}", args.seed + 1, 1000, 16184, 80882,
                                               choices=[5, 10, 20, 30, 50], passes=1)
+    if world == 1 and "intpoly" in sections:
+        forms["intpoly"] = section_intpoly(ctx, args.seed + 3)
     if world == 1 and "serving" in sections:
         forms["serving"] = section_serving(ctx, args.seed + 2)
 
@@ -458,7 +511,7 @@ def main():
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="trlwe_full")
     ap.add_argument("--seed", type=int, default=0x1DA52019)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--sections", default="plain,lwe_full,batched_uneven,serving",
+    ap.add_argument("--sections", default="plain,lwe_full,batched_uneven,intpoly,serving",
                     help="extra forms measured after the headline (comma list, '' for none)")
     args = ap.parse_args()
     args.steps_given = args.steps is not None
