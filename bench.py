@@ -365,6 +365,39 @@ def section_serving(ctx, seed, n_requests=10000, budget=150 << 30, inflight=4):
                         "request ciphertexts generated on the device"}
 
 
+def run_sections(ctx, args, sections):
+    """The forms beside the headline.  --small shrinks the LWE forms to
+    100 individuals x 2,000 tags x 10,000 targets (a few GB on the device),
+    the size the ncu captures under profiles/ use."""
+    ni, nt, ng = (100, 2000, 10000) if args.small else (1000, 16184, 80882)
+    scale = f"{ni:,} individuals x {ng:,} targets x 3, {nt:,} tags"
+    forms = {}
+    if "lwe_full" in sections:
+        forms["lwe_full"] = section_lwe(ctx, f"per-individual LWE: {scale}, 5 neighbours, n=1024", args.seed,
+                                        ni, nt, ng, neighbours=5)
+    if "batched_uneven" in sections:
+        forms["batched_uneven"] = section_lwe(ctx, f"batched uneven neighbourhoods, per-individual LWE: {scale}, "
+                                                   "neighbours uniform from {5,10,20,30,50}", args.seed + 1,
+                                              ni, nt, ng, choices=[5, 10, 20, 30, 50], passes=1)
+    if "intpoly" in sections:
+        forms["intpoly"] = section_intpoly(ctx, args.seed + 3)
+    if "serving" in sections:
+        forms["serving"] = section_serving(ctx, args.seed + 2)
+    return forms
+
+
+def run_sections_only(args):
+    """--no-headline: only the listed sections, one JSON line of forms."""
+    import torch
+    from idash2019_2_gb300 import gpu
+    torch.cuda.init()
+    ctx = gpu.Context(0)
+    sections = set(args.sections.split(",")) if args.sections else set()
+    forms = run_sections(ctx, args, sections)
+    ctx.close()
+    print(json.dumps({"metric": METRIC, "unit": UNIT, "forms": forms}), flush=True)
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -467,19 +500,8 @@ def run_ours(args):
     d_in.free()
     d_out.free()
     model.free()
-    if world == 1 and "lwe_full" in sections:
-        forms["lwe_full"] = section_lwe(ctx, "full scale, per-individual LWE: 1,000 individuals x 80,882 targets "
-                                             "x 3, 16,184 tags, 5 neighbours, n=1024", args.seed, 1000, 16184, 80882,
-                                        neighbours=5)
-    if world == 1 and "batched_uneven" in sections:
-        forms["batched_uneven"] = section_lwe(ctx, "batched uneven neighbourhoods, per-individual LWE: 1,000 "
-                                                   "individuals x 80,882 targets x 3, neighbours uniform from "
-                                                   "{5,10,20,30,50}", args.seed + 1, 1000, 16184, 80882,
-                                              choices=[5, 10, 20, 30, 50], passes=1)
-    if world == 1 and "intpoly" in sections:
-        forms["intpoly"] = section_intpoly(ctx, args.seed + 3)
-    if world == 1 and "serving" in sections:
-        forms["serving"] = section_serving(ctx, args.seed + 2)
+    if world == 1:
+        forms.update(run_sections(ctx, args, sections - {"plain"}))
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -513,12 +535,17 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--sections", default="plain,lwe_full,batched_uneven,intpoly,serving",
                     help="extra forms measured after the headline (comma list, '' for none)")
+    ap.add_argument("--no-headline", action="store_true",
+                    help="measure only --sections (no headline, e2e or CPU baseline)")
+    ap.add_argument("--small", action="store_true", help="LWE sections at a reduced size (profiling)")
     args = ap.parse_args()
     args.steps_given = args.steps is not None
     if args.steps is None:
         args.steps = 2000
     if args.impl == "reference":
         run_reference(args)
+    elif args.no_headline:
+        run_sections_only(args)
     else:
         run_ours(args)
 

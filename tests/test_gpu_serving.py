@@ -20,7 +20,8 @@ def served():
     for i in range(10):
         length = int(rng.integers(20, 400))
         t0 = int(rng.integers(0, 1000 - length))
-        reqs.append(dict(arrival_s=0.0003 * i, n_indiv=int(rng.integers(1, 2600)), target_begin=t0,
+        # arriving together: four are admitted at once and share the device
+        reqs.append(dict(arrival_s=0.0, n_indiv=int(rng.integers(1, 2600)), target_begin=t0,
                          target_end=t0 + length, seed=1000 + i))
     res, outs = m.serve(reqs, hbm_budget=2 << 30, max_inflight=4, keep_outputs=True)
     yield ctx, w, m, reqs, res, outs
