@@ -97,7 +97,8 @@ class ServeConfig(C.Structure):
 
 class CloudReport(C.Structure):
     _fields_ = [("read_s", C.c_double), ("plan_s", C.c_double), ("score_s", C.c_double),
-                ("write_s", C.c_double), ("n_in_records", C.c_uint64), ("n_out_records", C.c_uint64)]
+                ("write_s", C.c_double), ("n_in_records", C.c_uint64), ("n_out_records", C.c_uint64),
+                ("model_from_cache", C.c_uint32), ("reserved", C.c_uint32)]
 
 
 # name -> (restype, argtypes); every function include/idash_gpu.h declares.

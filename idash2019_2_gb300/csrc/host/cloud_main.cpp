@@ -3,7 +3,9 @@
 // log scrapers (eval/parse_log.py) keep working:
 //   idash_cloud [model_dir]   in a directory holding params.bin and
 //                             encrypted_data.bin; writes encrypted_prediction.bin.
-// Optional: IDASH_DEVICE (CUDA device ordinal, default 0).
+// Optional: IDASH_DEVICE (CUDA device ordinal, default 0); IDASH_MODEL_CACHE
+// (file holding the flattened model, read when it matches params.bin and the
+// model directory, written otherwise).
 #include <sys/resource.h>
 
 #include <chrono>
@@ -35,14 +37,18 @@ int main(int argc, char **argv) {
     }
     IdashParams params;
     Model model;
+    FlatModel flat;
     EncryptedData data;
     EncryptedPredictions preds;
+    const char *cache_env = std::getenv("IDASH_MODEL_CACHE");
+    bool cached = false;
     Status st = read_params(params, "params.bin");
-    if (st.ok()) st = read_model(model, params, model_dir);
+    if (st.ok()) st = load_model(&model, &flat, params, "params.bin", model_dir, cache_env ? cache_env : "", &cached);
     if (st.ok()) st = read_encrypted_data(data, params, "encrypted_data.bin");
+    if (cached) std::cout << "model from cache: " << cache_env << std::endl;
     const double t_start = wall();
     CloudTiming tm;
-    if (st.ok()) st = cloud_compute_score(preds, data, model, params, ctx, &tm);
+    if (st.ok()) st = cloud_compute_score(preds, data, flat, params, ctx, &tm);
     const double t_end = wall();
     if (st.ok()) st = write_encrypted_predictions(preds, "encrypted_prediction.bin");
     const double t_write = wall();

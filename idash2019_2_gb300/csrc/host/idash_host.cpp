@@ -247,10 +247,8 @@ Status write_encrypted_predictions(const EncryptedPredictions &preds, const std:
     return Status::Ok();
 }
 
-Status cloud_compute_score(EncryptedPredictions &preds, const EncryptedData &data, const Model &model,
-                           const IdashParams &params, idash_ctx *ctx, CloudTiming *timing) {
-    if (!preds.record_of.empty()) return Status::Err(IDASH_ERR_STATE, "predictions must be empty on entry");
-    const double t0 = now_s();
+FlatModel flatten_model(const Model &model) {
+    FlatModel f;
     // Record order of the output file: the reference creates one sample per
     // model entry in model-iteration order (eval/idash.cpp:772-777) in an
     // unordered_map and writes that map in its iteration order (:607).
@@ -259,25 +257,130 @@ Status cloud_compute_score(EncryptedPredictions &preds, const EncryptedData &dat
     uint64_t rec = 0;
     for (auto &it : score) it.second = rec++;
     const uint64_t n_out = score.size();
-
     // Outputs numbered by FeatBigIndex (neighbouring targets adjacent); each
     // output's terms in the model map's iteration order (the variance sum
     // order of eval/idash.cpp:800-819).
-    std::vector<FeatBigIndex> outs;
-    outs.reserve(n_out);
-    for (const auto &it : model.model) outs.push_back(it.first);
-    std::sort(outs.begin(), outs.end());
-    std::vector<uint64_t> term_ptr(n_out + 1, 0);
-    std::vector<uint32_t> term_feat, out_row(n_out);
-    std::vector<int32_t> term_coef;
+    f.out_bidx.reserve(n_out);
+    for (const auto &it : model.model) f.out_bidx.push_back(it.first);
+    std::sort(f.out_bidx.begin(), f.out_bidx.end());
+    f.term_ptr.assign(n_out + 1, 0);
+    f.out_row.resize(n_out);
     for (uint64_t o = 0; o < n_out; ++o) {
-        for (const auto &t : model.model.at(outs[o])) {
-            term_feat.push_back(t.first);
-            term_coef.push_back(t.second);
+        for (const auto &t : model.model.at(f.out_bidx[o])) {
+            f.term_feat.push_back(t.first);
+            f.term_coef.push_back(t.second);
         }
-        term_ptr[o + 1] = term_feat.size();
-        out_row[o] = uint32_t(score.at(outs[o]));
+        f.term_ptr[o + 1] = f.term_feat.size();
+        f.out_row[o] = uint32_t(score.at(f.out_bidx[o]));
     }
+    return f;
+}
+
+namespace {
+constexpr char kCacheMagic[8] = {'I', 'D', 'A', 'S', 'H', 'F', 'M', '1'};
+
+uint64_t fnv1a(uint64_t h, const void *data, size_t n) {
+    const uint8_t *p = static_cast<const uint8_t *>(data);
+    for (size_t i = 0; i < n; ++i) h = (h ^ p[i]) * 0x100000001B3ull;
+    return h;
+}
+}  // namespace
+
+uint64_t fingerprint(const std::string &params_file, const std::string &model_dir) {
+    uint64_t h = 0xCBF29CE484222325ull;
+    FILE *f = std::fopen(params_file.c_str(), "rb");
+    if (f) {
+        char buf[1 << 16];
+        size_t n;
+        while ((n = std::fread(buf, 1, sizeof(buf), f)) > 0) h = fnv1a(h, buf, n);
+        std::fclose(f);
+    }
+    return fnv1a(h, model_dir.data(), model_dir.size());
+}
+
+Status write_model_cache(const FlatModel &flat, uint64_t fp, const std::string &path) {
+    const std::string tmp = path + ".tmp";
+    FILE *f = std::fopen(tmp.c_str(), "wb");
+    if (!f) return Status::Err(IDASH_ERR_IO, "cannot write model cache '" + tmp + "'");
+    const uint64_t hdr[3] = {fp, flat.out_bidx.size(), flat.term_feat.size()};
+    bool ok = std::fwrite(kCacheMagic, 1, 8, f) == 8 && std::fwrite(hdr, 8, 3, f) == 3;
+    auto put = [&](const void *d, size_t bytes) { ok = ok && (bytes == 0 || std::fwrite(d, 1, bytes, f) == bytes); };
+    put(flat.out_bidx.data(), flat.out_bidx.size() * 4);
+    put(flat.out_row.data(), flat.out_row.size() * 4);
+    put(flat.term_ptr.data(), flat.term_ptr.size() * 8);
+    put(flat.term_feat.data(), flat.term_feat.size() * 4);
+    put(flat.term_coef.data(), flat.term_coef.size() * 4);
+    ok = (std::fclose(f) == 0) && ok;
+    if (!ok || std::rename(tmp.c_str(), path.c_str()) != 0) {
+        std::remove(tmp.c_str());
+        return Status::Err(IDASH_ERR_IO, "cannot write model cache '" + path + "'");
+    }
+    return Status::Ok();
+}
+
+Status read_model_cache(FlatModel *flat, uint64_t fp, const std::string &path) {
+    FILE *f = std::fopen(path.c_str(), "rb");
+    if (!f) return Status::Err(IDASH_ERR_IO, "no model cache at '" + path + "'");
+    char magic[8];
+    uint64_t hdr[3];
+    bool ok = std::fread(magic, 1, 8, f) == 8 && std::memcmp(magic, kCacheMagic, 8) == 0 &&
+              std::fread(hdr, 8, 3, f) == 3;
+    if (ok && hdr[0] != fp) {
+        std::fclose(f);
+        return Status::Err(IDASH_ERR_FORMAT, "model cache is for other params/model");
+    }
+    if (ok && (hdr[1] > (1ull << 32) || hdr[2] > (1ull << 40))) ok = false;
+    if (ok) {
+        flat->out_bidx.resize(hdr[1]);
+        flat->out_row.resize(hdr[1]);
+        flat->term_ptr.resize(hdr[1] + 1);
+        flat->term_feat.resize(hdr[2]);
+        flat->term_coef.resize(hdr[2]);
+    }
+    auto get = [&](void *d, size_t bytes) { ok = ok && (bytes == 0 || std::fread(d, 1, bytes, f) == bytes); };
+    get(flat->out_bidx.data(), hdr[1] * 4);
+    get(flat->out_row.data(), hdr[1] * 4);
+    get(flat->term_ptr.data(), (hdr[1] + 1) * 8);
+    get(flat->term_feat.data(), hdr[2] * 4);
+    get(flat->term_coef.data(), hdr[2] * 4);
+    std::fclose(f);
+    if (!ok || flat->term_ptr.back() != hdr[2]) return Status::Err(IDASH_ERR_FORMAT, "model cache is damaged");
+    return Status::Ok();
+}
+
+Status load_model(Model *parsed, FlatModel *flat, const IdashParams &params, const std::string &params_file,
+                  const std::string &model_dir, const std::string &cache_path, bool *from_cache) {
+    *from_cache = false;
+    uint64_t fp = 0;
+    if (!cache_path.empty()) {
+        fp = fingerprint(params_file, model_dir);
+        if (read_model_cache(flat, fp, cache_path).ok()) {
+            *from_cache = true;
+            return Status::Ok();
+        }
+    }
+    Status st = read_model(*parsed, params, model_dir);
+    if (!st.ok()) return st;
+    *flat = flatten_model(*parsed);
+    if (!cache_path.empty()) write_model_cache(*flat, fp, cache_path);  // best effort
+    return Status::Ok();
+}
+
+Status cloud_compute_score(EncryptedPredictions &preds, const EncryptedData &data, const Model &model,
+                           const IdashParams &params, idash_ctx *ctx, CloudTiming *timing) {
+    const double t0 = now_s();
+    const FlatModel flat = flatten_model(model);
+    const double t_flat = now_s() - t0;
+    Status st = cloud_compute_score(preds, data, flat, params, ctx, timing);
+    if (st.ok() && timing) timing->plan_s += t_flat;
+    return st;
+}
+
+Status cloud_compute_score(EncryptedPredictions &preds, const EncryptedData &data, const FlatModel &flat,
+                           const IdashParams &params, idash_ctx *ctx, CloudTiming *timing) {
+    if (!preds.record_of.empty()) return Status::Err(IDASH_ERR_STATE, "predictions must be empty on entry");
+    const double t0 = now_s();
+    const uint64_t n_out = flat.out_bidx.size();
     uint64_t n_index = 0;
     for (const auto &it : data.record_of) n_index = std::max<uint64_t>(n_index, uint64_t(it.first) + 1);
     std::vector<uint32_t> row_of_index(n_index, 0xFFFFFFFFu);
@@ -286,9 +389,9 @@ Status cloud_compute_score(EncryptedPredictions &preds, const EncryptedData &dat
     idash_trlwe_params tp{IdashParams::N, IdashParams::k, params.NUM_SAMPLES, params.NUM_REGIONS,
                           params.REGION_SIZE, IdashParams::ONE_IN_T32, kTlweSampleTag};
     idash_model *m = nullptr;
-    idash_status s = idash_model_trlwe(ctx, &m, &tp, n_out, outs.data(), out_row.data(), term_ptr.data(),
-                                       term_feat.data(), term_coef.data(), n_index, row_of_index.data(),
-                                       data.image.count);
+    idash_status s = idash_model_trlwe(ctx, &m, &tp, n_out, flat.out_bidx.data(), flat.out_row.data(),
+                                       flat.term_ptr.data(), flat.term_feat.data(), flat.term_coef.data(), n_index,
+                                       row_of_index.data(), data.image.count);
     if (s != IDASH_OK) return Status::Err(s, idash_last_error(ctx));
     const double t1 = now_s();
 
@@ -313,7 +416,7 @@ Status cloud_compute_score(EncryptedPredictions &preds, const EncryptedData &dat
     if (!st.ok()) return st;
     std::memcpy(preds.image.data, &preds.image.count, 8);
     preds.record_of.clear();
-    for (const auto &it : score) preds.record_of.emplace(it.first, it.second);
+    for (uint64_t o = 0; o < n_out; ++o) preds.record_of.emplace(flat.out_bidx[o], flat.out_row[o]);
     if (timing) {
         timing->plan_s = t1 - t0;
         timing->score_s = now_s() - t1;
@@ -340,14 +443,17 @@ extern "C" idash_status idash_cloud_files(int device, const char *params_file, c
     if (s != IDASH_OK) return fail(Status::Err(s, idash_last_error(nullptr)));
     IdashParams params;
     Model model;
+    FlatModel flat;
     EncryptedData data;
     EncryptedPredictions preds;
     CloudTiming tm;
+    const char *cache_env = std::getenv("IDASH_MODEL_CACHE");
+    bool cached = false;
     Status st = read_params(params, params_file);
-    if (st.ok()) st = read_model(model, params, model_dir);
+    if (st.ok()) st = load_model(&model, &flat, params, params_file, model_dir, cache_env ? cache_env : "", &cached);
     if (st.ok()) st = read_encrypted_data(data, params, data_file);
     const double t1 = now_s();
-    if (st.ok()) st = cloud_compute_score(preds, data, model, params, ctx, &tm);
+    if (st.ok()) st = cloud_compute_score(preds, data, flat, params, ctx, &tm);
     const double t2 = now_s();
     if (st.ok()) st = write_encrypted_predictions(preds, pred_file);
     const double t3 = now_s();
@@ -360,6 +466,7 @@ extern "C" idash_status idash_cloud_files(int device, const char *params_file, c
         report->write_s = t3 - t2;
         report->n_in_records = data.image.count;
         report->n_out_records = preds.image.count;
+        report->model_from_cache = cached ? 1 : 0;
     }
     if (errbuf && errbuf_len) errbuf[0] = '\0';
     return IDASH_OK;

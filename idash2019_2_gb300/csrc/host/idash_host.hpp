@@ -95,11 +95,40 @@ struct CloudTiming {
     double plan_s = 0, score_s = 0;  // model planning; copies + kernels
 };
 
+// The model as the GPU consumes it: outputs in FeatBigIndex order (so that
+// neighbouring targets share input windows), each output's terms in the
+// order the reference's map iterates them (the order of its variance sum,
+// eval/idash.cpp:800-819), and the record each output takes in
+// encrypted_prediction.bin (the order the reference writes, :607).
+struct FlatModel {
+    std::vector<FeatBigIndex> out_bidx;
+    std::vector<uint32_t> out_row;
+    std::vector<uint64_t> term_ptr;
+    std::vector<uint32_t> term_feat;
+    std::vector<int32_t> term_coef;
+};
+FlatModel flatten_model(const Model &model);
+
+// Model-ingest cache: the flattened model in one file, tagged with a
+// fingerprint of params.bin and the model directory's path.  Reading it
+// replaces parsing one .hr file per output (eval/idash.cpp:66-114).  The
+// cache does not watch the .hr files: remove it when they change.
+uint64_t fingerprint(const std::string &params_file, const std::string &model_dir);
+Status write_model_cache(const FlatModel &flat, uint64_t fp, const std::string &path);
+Status read_model_cache(FlatModel *flat, uint64_t fp, const std::string &path);
+
 // eval/idash.h:251-252 / eval/idash.cpp:763-848 on the GPU behind the C ABI.
 // `preds` must be empty on entry.  Records come out in the order the
 // reference's EncryptedPredictions map iterates, so the written file matches
 // the reference's byte for byte.
 Status cloud_compute_score(EncryptedPredictions &preds, const EncryptedData &data, const Model &model,
                            const IdashParams &params, idash_ctx *ctx, CloudTiming *timing = nullptr);
+Status cloud_compute_score(EncryptedPredictions &preds, const EncryptedData &data, const FlatModel &flat,
+                           const IdashParams &params, idash_ctx *ctx, CloudTiming *timing = nullptr);
+
+// params.bin, model (from the cache at cache_path when it is valid, else
+// parsed and, when cache_path is non-empty, cached there).
+Status load_model(Model *parsed, FlatModel *flat, const IdashParams &params, const std::string &params_file,
+                  const std::string &model_dir, const std::string &cache_path, bool *from_cache);
 
 }  // namespace idash_host

@@ -297,13 +297,18 @@ idash_status idash_score_trlwe_noalloc(const idash_trlwe_params *params, uint64_
  * the model directory of <pos>_<snp>.hr files (eval/idash.cpp:66-114) and
  * encrypted_data.bin (:513-535), scores on `device`, and writes
  * encrypted_prediction.bin (:596-613) with the records in the order the
- * reference writes them.  Ciphertext files move as single bulk images. */
+ * reference writes them.  Ciphertext files move as single bulk images.
+ * With IDASH_MODEL_CACHE=<file> in the environment the flattened model is
+ * read from that file when it matches params.bin and the model directory,
+ * and written there otherwise (remove it when the .hr files change). */
 typedef struct {
     double read_s;   /* params + model + ciphertext file reads */
     double plan_s;   /* model flattening and device planning */
     double score_s;  /* host->device copy, kernels, device->host copy */
     double write_s;  /* prediction file write */
     uint64_t n_in_records, n_out_records;
+    uint32_t model_from_cache; /* 1: the model came from the IDASH_MODEL_CACHE file */
+    uint32_t reserved;
 } idash_cloud_report;
 idash_status idash_cloud_files(int device, const char *params_file, const char *model_dir, const char *data_file,
                                const char *pred_file, idash_cloud_report *report, char *errbuf, size_t errbuf_len);

@@ -57,6 +57,29 @@ def test_cloud_files_hash_pinned_medium(tmp_path, name):
     assert hashlib.sha256(raw).hexdigest() == meta["sha256"]
 
 
+def test_model_cache_is_written_then_used(tmp_path, monkeypatch):
+    """IDASH_MODEL_CACHE: the first run parses the .hr files and writes the
+    flattened model; the second reads it; both outputs equal the reference's."""
+    src = copy_case("ref_r3_edge", tmp_path)
+    monkeypatch.setenv("IDASH_MODEL_CACHE", str(tmp_path / "model.cache"))
+    for expect_cached in (0, 1):
+        out = tmp_path / f"pred{expect_cached}.bin"
+        rep = gpu.cloud_files(str(tmp_path / "params.bin"), str(tmp_path / "model"),
+                              str(tmp_path / "encrypted_data.bin"), str(out))
+        assert rep["model_from_cache"] == expect_cached
+        assert filecmp.cmp(out, os.path.join(src, "encrypted_prediction.bin"), shallow=False)
+    # a cache for other params is ignored (and replaced)
+    (tmp_path / "params2.bin").write_bytes((tmp_path / "params.bin").read_bytes())
+    rep = gpu.cloud_files(str(tmp_path / "params2.bin"), str(tmp_path / "model"),
+                          str(tmp_path / "encrypted_data.bin"), str(tmp_path / "pred2.bin"))
+    assert rep["model_from_cache"] == 1  # same bytes, same directory: same fingerprint
+    (tmp_path / "model.cache").write_bytes(b"IDASHFM1" + b"\0" * 40)
+    rep = gpu.cloud_files(str(tmp_path / "params.bin"), str(tmp_path / "model"),
+                          str(tmp_path / "encrypted_data.bin"), str(tmp_path / "pred3.bin"))
+    assert rep["model_from_cache"] == 0
+    assert filecmp.cmp(tmp_path / "pred3.bin", os.path.join(src, "encrypted_prediction.bin"), shallow=False)
+
+
 def test_cloud_cli_matches_reference(tmp_path):
     src = copy_case("ref_r10", tmp_path)
     cli = os.path.join(ROOT, "idash2019_2_gb300", "idash_cloud")
