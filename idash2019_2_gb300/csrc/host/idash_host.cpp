@@ -438,9 +438,6 @@ extern "C" idash_status idash_cloud_files(int device, const char *params_file, c
     if (!params_file || !model_dir || !data_file || !pred_file)
         return fail(Status::Err(IDASH_ERR_INVALID_ARGUMENT, "null file name"));
     const double t0 = now_s();
-    idash_ctx *ctx = nullptr;
-    idash_status s = idash_open(&ctx, device);
-    if (s != IDASH_OK) return fail(Status::Err(s, idash_last_error(nullptr)));
     IdashParams params;
     Model model;
     FlatModel flat;
@@ -452,7 +449,11 @@ extern "C" idash_status idash_cloud_files(int device, const char *params_file, c
     Status st = read_params(params, params_file);
     if (st.ok()) st = load_model(&model, &flat, params, params_file, model_dir, cache_env ? cache_env : "", &cached);
     if (st.ok()) st = read_encrypted_data(data, params, data_file);
+    if (!st.ok()) return fail(st);  // every input is validated before the device is touched
     const double t1 = now_s();
+    idash_ctx *ctx = nullptr;
+    idash_status s = idash_open(&ctx, device);
+    if (s != IDASH_OK) return fail(Status::Err(s, idash_last_error(nullptr)));
     if (st.ok()) st = cloud_compute_score(preds, data, flat, params, ctx, &tm);
     const double t2 = now_s();
     if (st.ok()) st = write_encrypted_predictions(preds, pred_file);

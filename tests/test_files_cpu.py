@@ -1,0 +1,82 @@
+"""Failure handling of the cloud step's file inputs, without a GPU: every
+malformed input is an error status with a message (the reference aborts via
+REQUIRE_DRAMATICALLY, eval/idash.h:12), reported before the device is used."""
+import os
+import shutil
+
+import pytest
+
+from conftest import GOLDEN
+
+gpu = pytest.importorskip("idash2019_2_gb300.gpu")
+
+
+@pytest.fixture()
+def case(tmp_path):
+    try:
+        gpu._lib.load()
+    except ImportError as e:
+        pytest.skip(str(e))
+    src = os.path.join(GOLDEN, "ref_r10")
+    for f in ["params.bin", "encrypted_data.bin"]:
+        shutil.copy(os.path.join(src, f), tmp_path / f)
+    shutil.copytree(os.path.join(src, "model"), tmp_path / "model")
+    return tmp_path
+
+
+def run(d, params="params.bin", data="encrypted_data.bin"):
+    return gpu.cloud_files(str(d / params), str(d / "model"), str(d / data), str(d / "out.bin"), device=0)
+
+
+def expect(d, name, **kw):
+    with pytest.raises(gpu.IdashError) as e:
+        run(d, **kw)
+    assert e.value.name == name, str(e.value)
+    return str(e.value)
+
+
+def test_missing_params(case):
+    expect(case, "IDASH_ERR_IO", params="nope.bin")
+
+
+def test_truncated_params(case):
+    raw = (case / "params.bin").read_bytes()
+    (case / "params.bin").write_bytes(raw[:len(raw) // 2])
+    assert "truncated" in expect(case, "IDASH_ERR_FORMAT")
+
+
+def test_inconsistent_regions(case):
+    raw = bytearray((case / "params.bin").read_bytes())
+    raw[20:24] = (2048).to_bytes(4, "little")  # NUM_REGIONS * REGION_SIZE > N
+    (case / "params.bin").write_bytes(bytes(raw))
+    expect(case, "IDASH_ERR_FORMAT")
+
+
+def test_missing_model_file(case):
+    victim = sorted(os.listdir(case / "model"))[4]
+    os.remove(case / "model" / victim)
+    assert victim in expect(case, "IDASH_ERR_IO")
+
+
+def test_model_names_an_unknown_tag(case):
+    victim = sorted(os.listdir(case / "model"))[0]
+    with open(case / "model" / victim, "a") as f:
+        f.write("999999999_1 17\n")
+    expect(case, "IDASH_ERR_INDEX")
+
+
+def test_bad_feature_name(case):
+    victim = sorted(os.listdir(case / "model"))[1]
+    with open(case / "model" / victim, "a") as f:
+        f.write("notafeature 3\n")
+    expect(case, "IDASH_ERR_FORMAT")
+
+
+def test_truncated_ciphertexts(case):
+    raw = (case / "encrypted_data.bin").read_bytes()
+    (case / "encrypted_data.bin").write_bytes(raw[:-100])
+    assert "8208" in expect(case, "IDASH_ERR_FORMAT")
+
+
+def test_missing_ciphertexts(case):
+    expect(case, "IDASH_ERR_IO", data="absent.bin")
