@@ -49,14 +49,17 @@ idash_status upload(idash_ctx *ctx, T **dst, const std::vector<T> &src) {
 struct Candidate {
     KernelKind kind;
     uint32_t w, g, slots, terms, groups, cps;
+    uint32_t stages = 1;  // kWs: buffers in the ring
 };
 
 // Shared-memory carve-up of one buffer: a window-kernel CTA for `cps` CTAs
 // per SM, or one of the two buffers of a pipe-kernel CTA (one per SM).
-bool window_limits(const idash_ctx *ctx, KernelKind kind, uint32_t w, uint32_t cps, Candidate *c) {
+bool window_limits(const idash_ctx *ctx, KernelKind kind, uint32_t w, uint32_t cps, Candidate *c,
+                   uint32_t stages = 1) {
     const size_t per_sm = 233472;  // 228 KB of shared memory per SM
     size_t budget = std::min(per_sm / cps - kSmemReserve, ctx->smem_optin);
     if (kind == KernelKind::kPipe) budget = (budget - 128) / 2;
+    if (kind == KernelKind::kWs) budget = (budget - 128) / stages;
     const uint32_t groups = 64;
     const size_t fixed = 128 + size_t(groups) * sizeof(PlanGroup);
     if (budget <= fixed) return false;
@@ -67,7 +70,7 @@ bool window_limits(const idash_ctx *ctx, KernelKind kind, uint32_t w, uint32_t c
     uint32_t slots = uint32_t(left / (size_t(w) * 4));
     if (ctx->opt_max_window_slots > 0) slots = uint32_t(std::min<int64_t>(slots, ctx->opt_max_window_slots));
     if (slots == 0) return false;
-    *c = Candidate{kind, w, 3, slots, terms, groups, kind == KernelKind::kPipe ? 1u : cps};
+    *c = Candidate{kind, w, 3, slots, terms, groups, kind == KernelKind::kPipe ? 1u : cps, stages};
     return true;
 }
 
@@ -123,12 +126,13 @@ idash_status build_and_upload(idash_model *m, const Candidate &c) {
     m->kind = c.kind;
     m->slice_words = c.w;
     m->group_size = c.g;
+    m->n_stages = c.stages;
     m->max_slots = m->plan.max_block_slots;
     m->max_terms = m->plan.max_block_terms;
     m->max_groups = m->plan.max_block_groups;
     uint32_t cps = c.cps;
     if (c.kind != KernelKind::kDirect) {
-        const size_t smem = kernel_smem_bytes(c.kind, c.w, m->max_slots, m->max_terms, m->max_groups);
+        const size_t smem = kernel_smem_bytes(c.kind, c.w, m->max_slots, m->max_terms, m->max_groups, c.stages);
         const int occ = resident_ctas_per_sm(c.kind, c.w, c.g, smem);
         if (occ <= 0) return ctx->fail(IDASH_ERR_CUDA, "scoring kernel cannot be resident with this shared memory");
         cps = std::min<uint32_t>(cps ? cps : uint32_t(occ), uint32_t(occ));
@@ -169,6 +173,7 @@ ScoreArgs make_args(idash_model *m, const uint8_t *in_payload, uint64_t in_strid
     a.max_slots = m->max_slots;
     a.max_terms = m->max_terms;
     a.max_groups = m->max_groups;
+    a.n_stages = m->n_stages;
     a.tile_counter = m->ctx->counter();
     a.err = m->ctx->d_err;
     return a;
@@ -276,12 +281,17 @@ std::vector<Candidate> candidates(idash_model *m) {
     else cpss = {1, 2};
     const bool window = ctx->opt_kernel == 0 || ctx->opt_kernel == 2;
     const bool pipe = ctx->opt_kernel == 0 || ctx->opt_kernel == 3;
+    const bool use_ws = ctx->opt_kernel == 0 || ctx->opt_kernel == 4;
     for (uint32_t w : ws) {
         Candidate c;
         if (window)
             for (uint32_t cps : cpss)
                 if (window_limits(ctx, KernelKind::kWindow, w, cps, &c)) out.push_back(c);
         if (pipe && window_limits(ctx, KernelKind::kPipe, w, 1, &c)) out.push_back(c);
+        if (use_ws)
+            for (uint32_t cps : cpss)
+                for (uint32_t stages : {2u, 3u})
+                    if (window_limits(ctx, KernelKind::kWs, w, cps, &c, stages)) out.push_back(c);
     }
     return out;
 }
@@ -440,7 +450,7 @@ idash_status idash_set_option(idash_ctx *ctx, const char *name, int64_t value) {
     if (!ctx || !name) return IDASH_ERR_INVALID_ARGUMENT;
     const std::string n(name);
     if (n == "kernel") {
-        if (value < 0 || value > 3) return ctx->fail(IDASH_ERR_INVALID_ARGUMENT, "kernel must be 0, 1, 2 or 3");
+        if (value < 0 || value > 4) return ctx->fail(IDASH_ERR_INVALID_ARGUMENT, "kernel must be 0 .. 4");
         ctx->opt_kernel = value;
     } else if (n == "slice_words") {
         if (value != 0 && !slice_supported(uint32_t(value)))

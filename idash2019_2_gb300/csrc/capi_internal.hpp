@@ -90,6 +90,7 @@ struct idash_model {
     idash::Plan plan;
     idash::KernelKind kind = idash::KernelKind::kWindow;
     uint32_t slice_words = 1024, group_size = 3;
+    uint32_t n_stages = 1;  // warp-specialised kernel's ring depth
     uint32_t max_slots = 0, max_terms = 0, max_groups = 0;
     uint32_t ctas = 0;
     bool tuned = false;

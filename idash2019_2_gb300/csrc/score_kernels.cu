@@ -379,6 +379,129 @@ __global__ void __launch_bounds__(kPipeThreads, 1) k_score_pipe(const ScoreArgs 
     }
 }
 
+constexpr int kWsConsumers = 8;                    // consumer warps per CTA
+constexpr int kWsThreads = (kWsConsumers + 1) * 32;  // + one producer warp
+constexpr uint32_t kWsMaxStages = 4;
+
+// k_score_ws (batched, warp-specialised): one producer warp fills a ring of
+// shared-memory stages (tile header + window + terms + groups) with bulk
+// copies and signals `full[s]`; eight consumer warps each take their groups
+// of the tile in a stage, accumulate, store, and arrive on `empty[s]`.  No
+// CTA-wide barrier: loads of the next stages overlap the arithmetic of the
+// current one, and a warp that finishes early moves on to the next stage.
+template <int W, int G, int Q>
+__global__ void __launch_bounds__(kWsThreads) k_score_ws(const ScoreArgs a) {
+    constexpr int TEAM = W / (4 * Q);
+    constexpr int NTEAMS = kWsConsumers * 32 / TEAM;
+    static_assert(TEAM >= 32 && (kWsConsumers * 32) % TEAM == 0, "a team is one or more whole warps");
+    extern __shared__ __align__(128) uint8_t smem[];
+    const uint32_t n_stages = a.n_stages;
+    uint64_t *full = reinterpret_cast<uint64_t *>(smem);               // [kWsMaxStages]
+    uint64_t *empty = full + kWsMaxStages;                              // [kWsMaxStages]
+    uint32_t *tile_of = reinterpret_cast<uint32_t *>(empty + kWsMaxStages);  // [kWsMaxStages]
+    const uint32_t buf_bytes = a.max_slots * W * 4 + a.max_terms * uint32_t(sizeof(PlanTerm)) +
+                               a.max_groups * uint32_t(sizeof(PlanGroup));
+    const uint32_t terms_off = a.max_slots * W * 4;
+    const uint32_t groups_off = terms_off + a.max_terms * uint32_t(sizeof(PlanTerm));
+    auto win_of = [&](uint32_t s) { return reinterpret_cast<uint32_t *>(smem + 128 + s * buf_bytes); };
+    auto terms_of = [&](uint32_t s) { return reinterpret_cast<PlanTerm *>(smem + 128 + s * buf_bytes + terms_off); };
+    auto groups_of = [&](uint32_t s) {
+        return reinterpret_cast<PlanGroup *>(smem + 128 + s * buf_bytes + groups_off);
+    };
+    const uint32_t warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+    if (threadIdx.x == 0) {
+        for (uint32_t s = 0; s < n_stages; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], kWsConsumers);
+        }
+        fence_mbar_init();
+    }
+    __syncthreads();
+
+    if (warp == kWsConsumers) {
+        // ------------------------------------------------------------ producer
+        uint32_t pending = 0;  // stages with copies not yet consumed
+        uint32_t it = 0;
+        for (;; ++it) {
+            const uint32_t s = it % n_stages, round = it / n_stages;
+            if (round > 0) {
+                bool ok = true;
+                if (lane == 0) ok = mbar_wait_bounded(&empty[s], (round - 1) & 1u, a.err);
+                ok = __shfl_sync(0xFFFFFFFFu, ok ? 1 : 0, 0) != 0;
+                if (!ok) break;
+                pending &= ~(1u << s);
+            }
+            uint32_t tile = 0;
+            if (lane == 0) tile = atomicAdd(a.tile_counter, 1u);
+            tile = __shfl_sync(0xFFFFFFFFu, tile, 0);
+            if (lane == 0) tile_of[s] = tile;
+            if (tile >= a.n_tiles) {
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&full[s]);  // end-of-work marker
+                return;
+            }
+            const PlanBlock blk = a.blocks[a.block_lo + tile % a.n_blocks];
+            const uint32_t c0 = (tile / a.n_blocks) * W;
+            const uint32_t valid = min(uint32_t(W), a.row_words - c0);
+            uint32_t *win = win_of(s);
+            // rotated slots (NUM_REGIONS > 1): gathered by the producer lanes
+            for (uint32_t sl_i = uint32_t(blk.n_slots) - blk.n_rot; sl_i < blk.n_slots; ++sl_i) {
+                const PlanSlot sl = a.slots[blk.slot_begin + sl_i];
+                if (sl.row - a.row_base >= a.n_rows) continue;
+                const uint32_t *src =
+                    reinterpret_cast<const uint32_t *>(a.in + uint64_t(sl.row - a.row_base) * a.in_stride);
+                for (uint32_t x = lane; x < valid; x += 32) win[size_t(sl_i) * W + x] = rotated_word(src, c0 + x, sl.rot, a.N);
+            }
+            issue_tile_loads<W>(a, blk, c0, ((valid + 3u) & ~3u) * 4u, win, terms_of(s), groups_of(s), &full[s],
+                                lane);
+            pending |= 1u << s;
+        }
+        // A wait expired: let every copy this CTA issued land before exiting.
+        // The last n_stages iterations issued each stage's newest copies.
+        for (uint32_t k = 1; k <= n_stages && k <= it; ++k) {
+            const uint32_t j = it - k, sj = j % n_stages;
+            if (((pending >> sj) & 1u) && lane == 0) mbar_wait_bounded(&full[sj], (j / n_stages) & 1u, nullptr);
+        }
+        return;
+    }
+
+    // --------------------------------------------------------------- consumers
+    const uint32_t ctid = threadIdx.x;  // 0 .. 32*kWsConsumers-1
+    const uint32_t team = ctid / TEAM, tlane = ctid % TEAM;
+    for (uint32_t it = 0;; ++it) {
+        const uint32_t s = it % n_stages, round = it / n_stages;
+        if (!mbar_wait_bounded(&full[s], round & 1u, a.err)) return;
+        const uint32_t tile = tile_of[s];
+        if (tile >= a.n_tiles) return;
+        const PlanBlock blk = a.blocks[a.block_lo + tile % a.n_blocks];
+        const uint32_t c0 = (tile / a.n_blocks) * W;
+        const uint32_t valid = min(uint32_t(W), a.row_words - c0);
+        uint32_t bias_mask, zero_mask;
+        column_masks<Q, TEAM>(a, c0, tlane, bias_mask, zero_mask);
+        const uint32_t *wlane = win_of(s) + 4 * tlane;
+        const PlanTerm *terms_s = terms_of(s);
+        const PlanGroup *groups_s = groups_of(s);
+        for (uint32_t g = team; g < blk.n_groups; g += NTEAMS) {
+            const PlanGroup gr = groups_s[g];
+            uint32_t acc[G][4 * Q];
+            init_acc<G, Q>(acc, gr, bias_mask);
+            const PlanTerm *tp = terms_s + gr.term_begin;
+#pragma unroll 2
+            for (uint32_t t = 0; t < gr.n_terms; ++t) {
+                const PlanTerm tm = tp[t];
+                const uint32_t *w = wlane + size_t(tm.slot) * W;
+                uint4 x[Q];
+#pragma unroll
+                for (int k = 0; k < Q; ++k) x[k] = *reinterpret_cast<const uint4 *>(w + 4 * k * TEAM);
+                mac<G, Q>(acc, tm, x);
+            }
+            write_outputs<G, Q, TEAM>(a, gr, acc, c0, tlane, valid, zero_mask);
+        }
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&empty[s]);
+    }
+}
+
 template <int W, int G, int Q>
 __global__ void __launch_bounds__(kThreads) k_score_direct(const ScoreArgs a) {
     constexpr int TEAM = W / (4 * Q);
@@ -484,6 +607,15 @@ KernelFn pick(KernelKind kind, uint32_t w) {
                 case 2048: return k_score_pipe<2048, G, 4>;
             }
             break;
+        case KernelKind::kWs:
+            switch (w) {
+                case 128: return k_score_ws<128, G, 1>;
+                case 256: return k_score_ws<256, G, 2>;
+                case 512: return k_score_ws<512, G, 4>;
+                case 1024: return k_score_ws<1024, G, 4>;
+                case 2048: return k_score_ws<2048, G, 4>;
+            }
+            break;
         case KernelKind::kDirect:
             switch (w) {
                 case 128: return k_score_direct<128, G, 1>;
@@ -501,7 +633,9 @@ KernelFn pick_kernel(KernelKind kind, uint32_t w, uint32_t g) {
     return g == 1 ? pick<1>(kind, w) : g == 3 ? pick<3>(kind, w) : nullptr;
 }
 
-uint32_t threads_of(KernelKind kind) { return kind == KernelKind::kPipe ? kPipeThreads : kThreads; }
+uint32_t threads_of(KernelKind kind) {
+    return kind == KernelKind::kPipe ? kPipeThreads : kind == KernelKind::kWs ? kWsThreads : kThreads;
+}
 
 }  // namespace
 
@@ -513,17 +647,18 @@ size_t buffer_bytes(uint32_t slice_words, uint32_t max_slots, uint32_t max_terms
 }
 
 size_t kernel_smem_bytes(KernelKind kind, uint32_t slice_words, uint32_t max_slots, uint32_t max_terms,
-                         uint32_t max_groups) {
+                         uint32_t max_groups, uint32_t n_stages) {
     const size_t buf = buffer_bytes(slice_words, max_slots, max_terms, max_groups);
     switch (kind) {
         case KernelKind::kWindow: return 128 + buf;
         case KernelKind::kPipe: return 128 + 2 * buf;
+        case KernelKind::kWs: return 128 + size_t(n_stages) * buf;
         default: return 0;
     }
 }
 
 cudaError_t configure_window_kernels(size_t max_smem) {
-    for (KernelKind kind : {KernelKind::kWindow, KernelKind::kPipe})
+    for (KernelKind kind : {KernelKind::kWindow, KernelKind::kPipe, KernelKind::kWs})
         for (uint32_t w : {128u, 256u, 512u, 1024u, 2048u})
             for (uint32_t g : {1u, 3u}) {
                 cudaError_t e = cudaFuncSetAttribute(pick_kernel(kind, w, g),
@@ -550,7 +685,8 @@ cudaError_t launch_score(KernelKind kind, uint32_t slice_words, uint32_t group_s
     if (kind == KernelKind::kDirect) {
         fn<<<a.n_tiles, kThreads, 0, stream>>>(a);
     } else {
-        const size_t smem = kernel_smem_bytes(kind, slice_words, a.max_slots, a.max_terms, a.max_groups);
+        if (kind == KernelKind::kWs && (a.n_stages < 2 || a.n_stages > kWsMaxStages)) return cudaErrorInvalidValue;
+        const size_t smem = kernel_smem_bytes(kind, slice_words, a.max_slots, a.max_terms, a.max_groups, a.n_stages);
         cudaError_t e = cudaMemsetAsync(a.tile_counter, 0, sizeof(uint32_t), stream);
         if (e != cudaSuccess) return e;
         fn<<<ctas < a.n_tiles ? ctas : a.n_tiles, threads_of(kind), smem, stream>>>(a);

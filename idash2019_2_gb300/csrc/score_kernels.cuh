@@ -32,7 +32,8 @@ struct ScoreArgs {
     uint32_t form;                // kFormTrlwe / kFormLwe
     uint32_t N, num_samples, region_size;  // TRLWE epilogue
     uint32_t lwe_n1;                       // LWE: n + 1 words per sample
-    uint32_t max_slots, max_terms, max_groups;  // shared-memory carve-up
+    uint32_t max_slots, max_terms, max_groups;  // shared-memory carve-up (one buffer)
+    uint32_t n_stages;                          // warp-specialised kernel: buffers in the ring
     uint32_t *tile_counter;       // persistent kernel: next tile (zeroed before launch)
     uint32_t *err;                // device error word
 };
@@ -41,16 +42,20 @@ struct ScoreArgs {
 // kDirect: one CTA per tile, inputs read from global memory (plain form).
 // kPipe:   persistent, 512 threads, two buffers (next tile loads while the
 //          current one computes), one CTA per SM.
-enum class KernelKind : int { kWindow = 0, kDirect = 1, kPipe = 2 };
+// kWs:     persistent, warp-specialised: 1 producer + 8 consumer warps over a
+//          ring of n_stages buffers handed over with mbarriers.
+enum class KernelKind : int { kWindow = 0, kDirect = 1, kPipe = 2, kWs = 3 };
+constexpr uint32_t kMaxStages = 4;
 
 // Slice widths the kernels are instantiated for.
 bool slice_supported(uint32_t slice_words);
 
 // One shared-memory buffer (window + terms + groups) for the given limits.
 size_t buffer_bytes(uint32_t slice_words, uint32_t max_slots, uint32_t max_terms, uint32_t max_groups);
-// Dynamic shared memory of one CTA of `kind` (0 for the direct kernel).
+// Dynamic shared memory of one CTA of `kind` (0 for the direct kernel);
+// n_stages counts the kWs ring's buffers.
 size_t kernel_smem_bytes(KernelKind kind, uint32_t slice_words, uint32_t max_slots, uint32_t max_terms,
-                         uint32_t max_groups);
+                         uint32_t max_groups, uint32_t n_stages = 1);
 inline size_t window_smem_bytes(uint32_t slice_words, uint32_t max_slots, uint32_t max_terms, uint32_t max_groups) {
     return kernel_smem_bytes(KernelKind::kWindow, slice_words, max_slots, max_terms, max_groups);
 }

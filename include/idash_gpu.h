@@ -71,7 +71,8 @@ idash_status idash_sync(idash_ctx *ctx);
 
 /* Tunables: "kernel" (0 batched: autotuned among the persistent kernels,
  * 1 plain per-output kernel, 2 single-buffer persistent only, 3 double-buffer
- * persistent only), "slice_words" (0 = autotune; 128..2048), "ctas_per_sm",
+ * persistent only, 4 warp-specialised producer/consumer ring only),
+ * "slice_words" (0 = autotune; 128..2048), "ctas_per_sm",
  * "graph" (0/1: replay launches from a CUDA graph), "max_window_slots",
  * "max_group_terms". */
 idash_status idash_set_option(idash_ctx *ctx, const char *name, int64_t value);

@@ -115,8 +115,11 @@ def test_trlwe_synth_vs_oracle(ctx, oracle, regions, kernel):
     np.testing.assert_array_equal(got, want)
 
 
+KIND_OF_OPTION = {2: 0, 3: 2, 4: 3}  # "kernel" option -> idash_model_info.kernel
+
+
 @pytest.mark.parametrize("slice_words", [128, 256, 512, 1024, 2048])
-@pytest.mark.parametrize("kernel,graph", [(2, 0), (2, 1), (3, 1)])
+@pytest.mark.parametrize("kernel,graph", [(2, 0), (2, 1), (3, 1), (4, 0), (4, 1)])
 def test_trlwe_device_path_tiles(ctx, oracle, slice_words, kernel, graph):
     """Every slice width of the single-buffer (2) and double-buffer (3)
     persistent kernels, with and without graph replay, on the
@@ -142,7 +145,7 @@ def test_trlwe_device_path_tiles(ctx, oracle, slice_words, kernel, graph):
                                          1024)
             np.testing.assert_array_equal(got, want)
         assert m.info()["slice_words"] == slice_words
-        assert m.info()["kernel"] == (0 if kernel == 2 else 2)
+        assert m.info()["kernel"] == KIND_OF_OPTION[kernel]
         m.free()
     finally:
         ctx.set_option("slice_words", 0)
@@ -150,7 +153,7 @@ def test_trlwe_device_path_tiles(ctx, oracle, slice_words, kernel, graph):
         ctx.set_option("kernel", 0)
 
 
-@pytest.mark.parametrize("kernel", [2, 3])
+@pytest.mark.parametrize("kernel", [2, 3, 4])
 def test_trlwe_regions_persistent_kernels(ctx, oracle, kernel):
     """NUM_REGIONS = 10 (rotated slots gathered in shared memory) on both
     persistent kernels with a graph."""
@@ -203,7 +206,8 @@ def test_trlwe_autotune_picks_a_correct_plan(ctx, oracle):
     assert info["kernel"] in (0, 2) and info["slice_words"] in (512, 1024, 2048)
 
 
-@pytest.mark.parametrize("kernel,slice_words", [(0, 0), (2, 128), (3, 256), (3, 512), (1, 256)])
+@pytest.mark.parametrize("kernel,slice_words", [(0, 0), (2, 128), (3, 256), (3, 512), (1, 256), (4, 256),
+                                                (4, 1024)])
 def test_lwe_vs_oracle_ranges(ctx, oracle, kernel, slice_words):
     n, n_indiv, n_tags = 1024, 37, 60
     w = gpu.synth_model(seed=9, n_tags=n_tags, n_targets=90, choices=[5, 10, 2])
