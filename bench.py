@@ -45,6 +45,22 @@ WORKLOADS = {
 }
 METRIC = "encrypted predictions/s (indiv x target x 3)"
 UNIT = "predictions/s"
+KERNEL_NAMES = {0: "window (batched, persistent, CUDA graph)", 1: "direct (plain)",
+                2: "pipe (batched, double-buffered, persistent, CUDA graph)",
+                3: "ws (batched, warp-specialised producer + consumers over an mbarrier ring, CUDA graph)"}
+
+
+class timed_range:
+    """NVTX push/pop range 'timed' around a timed region, so that a profiler
+    can be limited to it (ncu --nvtx --nvtx-include timed/)."""
+
+    def __enter__(self):
+        import torch
+        torch.cuda.nvtx.range_push("timed")
+
+    def __exit__(self, *exc):
+        import torch
+        torch.cuda.nvtx.range_pop()
 
 
 def peaks():
@@ -191,8 +207,9 @@ def time_on_stream(ctx, fn, steps):
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     ctx.sync()
     e0.record(stream)
-    for _ in range(steps):
-        fn()
+    with timed_range():
+        for _ in range(steps):
+            fn()
     e1.record(stream)
     e1.synchronize()
     ctx.sync()
@@ -252,7 +269,7 @@ def section_lwe(ctx, name, seed, n_indiv, n_tags, n_targets, neighbours=5, choic
            "individuals": n_indiv, "targets": n_targets, "tags": n_tags,
            "neighbours": neighbours if not choices else f"uniform from {choices}",
            "input_bytes": n_feat * stride * 4, "output_bytes_per_step": m.n_out * L * 4,
-           "kernel": "window (batched, persistent)" if info["kernel"] == 0 else "direct",
+           "kernel": KERNEL_NAMES.get(info["kernel"], str(info["kernel"])),
            "slice_words": info["slice_words"], "launches_per_step": launches,
            "first_pass_s_including_autotune": first_s,
            "roofline": {"bound": "hbm", "achieved": alg / (ms / 1e3) / 1e9, "peak": peak, "unit": "GB/s",
@@ -434,8 +451,9 @@ def run_ours(args):
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     t0 = time.time()
     e0.record(stream)
-    for _ in range(args.steps):
-        model.score_device(d_in.ptr, lay, d_out.ptr, lay)
+    with timed_range():
+        for _ in range(args.steps):
+            model.score_device(d_in.ptr, lay, d_out.ptr, lay)
     e1.record(stream)
     e1.synchronize()
     t1 = time.time()
@@ -510,7 +528,7 @@ def run_ours(args):
                 "config": {"workload": spec["desc"], "individuals": spec["n_indiv"], "targets": spec["n_targets"],
                            "tags": spec["n_tags"], "neighbours": spec["neighbours"], "outputs": model.n_out,
                            "input_rows": spec["n_rows"], "l2": "inputs 0.40 GB and outputs 1.99 GB exceed the 129 MB L2",
-                           "kernel": "window (batched, persistent, CUDA graph)" if info["kernel"] == 0 else "direct",
+                           "kernel": KERNEL_NAMES.get(info["kernel"], str(info["kernel"])),
                            "slice_words": info["slice_words"], "parallelism": f"{world} independent batch(es)"},
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                              "frac": achieved / peak, "traffic": traffic, "peak_source": peak_src,
