@@ -234,6 +234,29 @@ def section_plain(ctx, w, spec, d_in, d_out, steps):
             "kernel": "direct: one output per team, every input read from global memory"}
 
 
+def section_kinds(ctx, w, spec, d_in, d_out, steps):
+    """Each batched kernel kind on the headline workload, autotuned within its
+    kind (slice width, CTAs per SM, ring depth)."""
+    from idash2019_2_gb300 import gpu
+    out = {}
+    lay = gpu.DENSE_TRLWE
+    for option, name in ((2, "window"), (3, "pipe"), (4, "ws")):
+        ctx.set_option("kernel", option)
+        try:
+            m = gpu.TrlweModel(ctx, w.model, spec["n_rows"], spec["num_samples"], spec["regions"],
+                               spec["region_size"])
+            for _ in range(3):
+                m.score_device(d_in.ptr, lay, d_out.ptr, lay)
+            ms = time_on_stream(ctx, lambda: m.score_device(d_in.ptr, lay, d_out.ptr, lay), steps)
+            info = m.info()
+            out[name] = {"ms_per_step": ms, "slice_words": info["slice_words"], "n_blocks": info["n_blocks"],
+                         "max_window_slots": info["max_window_slots"]}
+            m.free()
+        finally:
+            ctx.set_option("kernel", 0)
+    return out
+
+
 def section_lwe(ctx, name, seed, n_indiv, n_tags, n_targets, neighbours=5, choices=None, passes=2, chunk=2048):
     """Per-individual LWE form: inputs resident (n_indiv LWE samples of n=1024
     per feature row), outputs produced range by range into a 2-slot HBM ring
@@ -515,11 +538,13 @@ def run_ours(args):
     if world == 1 and "plain" in sections:
         forms["plain"] = section_plain(ctx, w, spec, d_in, d_out, min(args.steps, 200))
         forms["plain"]["batched_over_plain"] = value / forms["plain"]["value"]
+    if world == 1 and "kinds" in sections:
+        forms["kinds"] = section_kinds(ctx, w, spec, d_in, d_out, min(args.steps, 200))
     d_in.free()
     d_out.free()
     model.free()
     if world == 1:
-        forms.update(run_sections(ctx, args, sections - {"plain"}))
+        forms.update(run_sections(ctx, args, sections - {"plain", "kinds"}))
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,

@@ -59,7 +59,7 @@ bool window_limits(const idash_ctx *ctx, KernelKind kind, uint32_t w, uint32_t c
     const size_t per_sm = 233472;  // 228 KB of shared memory per SM
     size_t budget = std::min(per_sm / cps - kSmemReserve, ctx->smem_optin);
     if (kind == KernelKind::kPipe) budget = (budget - 128) / 2;
-    if (kind == KernelKind::kWs) budget = (budget - 128) / stages;
+    if (kind == KernelKind::kWs) budget = (budget - kWsHeaderBytes) / stages;
     const uint32_t groups = 64;
     const size_t fixed = 128 + size_t(groups) * sizeof(PlanGroup);
     if (budget <= fixed) return false;
@@ -288,10 +288,9 @@ std::vector<Candidate> candidates(idash_model *m) {
             for (uint32_t cps : cpss)
                 if (window_limits(ctx, KernelKind::kWindow, w, cps, &c)) out.push_back(c);
         if (pipe && window_limits(ctx, KernelKind::kPipe, w, 1, &c)) out.push_back(c);
-        if (use_ws)
-            for (uint32_t cps : cpss)
-                for (uint32_t stages : {2u, 3u})
-                    if (window_limits(ctx, KernelKind::kWs, w, cps, &c, stages)) out.push_back(c);
+        if (use_ws)  // one 512-thread CTA per SM (register file)
+            for (uint32_t stages : {2u, 3u})
+                if (window_limits(ctx, KernelKind::kWs, w, 1, &c, stages)) out.push_back(c);
     }
     return out;
 }

@@ -379,34 +379,49 @@ __global__ void __launch_bounds__(kPipeThreads, 1) k_score_pipe(const ScoreArgs 
     }
 }
 
-constexpr int kWsConsumers = 8;                    // consumer warps per CTA
+constexpr int kWsConsumers = 15;                     // consumer warps per CTA (512 threads: 128 registers each)
 constexpr int kWsThreads = (kWsConsumers + 1) * 32;  // + one producer warp
 constexpr uint32_t kWsMaxStages = 4;
 
-// k_score_ws (batched, warp-specialised): one producer warp fills a ring of
-// shared-memory stages (tile header + window + terms + groups) with bulk
-// copies and signals `full[s]`; eight consumer warps each take their groups
-// of the tile in a stage, accumulate, store, and arrive on `empty[s]`.  No
-// CTA-wide barrier: loads of the next stages overlap the arithmetic of the
-// current one, and a warp that finishes early moves on to the next stage.
+// Per-stage header written by the producer before it signals the stage full.
+struct WsStageHeader {
+    PlanBlock blk;       // the tile's block
+    uint32_t tile;       // tile index, >= n_tiles marks the end of work
+    uint32_t next_unit;  // work counter: consumers take (group, part) units from it
+    uint32_t pad[6];
+};
+static_assert(sizeof(WsStageHeader) == 64, "stage header layout");
+static_assert(2 * kWsMaxStages * 8 + kWsMaxStages * sizeof(WsStageHeader) <= kWsHeaderBytes,
+              "barriers and stage headers fit the header area");
+
+// k_score_ws (batched, warp-specialised): one CTA of 1 producer + 15 consumer
+// warps per SM.  The producer fills a ring of shared-memory stages (window +
+// terms + groups, with the tile's block header) by bulk copies and signals
+// `full[s]`.  Consumer warps take work units - one group's columns handled by
+// one warp (a TEAM / 32 part of the group's slice) - from the stage's shared
+// counter, so uneven groups balance across warps; a warp that runs out of
+// units arrives on `empty[s]` and moves on to the next stage.  No CTA-wide
+// barrier: the next stages' copies overlap this stage's arithmetic.
 template <int W, int G, int Q>
-__global__ void __launch_bounds__(kWsThreads) k_score_ws(const ScoreArgs a) {
+__global__ void __launch_bounds__(kWsThreads, 1) k_score_ws(const ScoreArgs a) {
     constexpr int TEAM = W / (4 * Q);
-    constexpr int NTEAMS = kWsConsumers * 32 / TEAM;
-    static_assert(TEAM >= 32 && (kWsConsumers * 32) % TEAM == 0, "a team is one or more whole warps");
+    constexpr int PARTS = TEAM / 32;  // warps per group-slice
+    static_assert(TEAM >= 32 && TEAM % 32 == 0, "a team is one or more whole warps");
     extern __shared__ __align__(128) uint8_t smem[];
     const uint32_t n_stages = a.n_stages;
-    uint64_t *full = reinterpret_cast<uint64_t *>(smem);               // [kWsMaxStages]
-    uint64_t *empty = full + kWsMaxStages;                              // [kWsMaxStages]
-    uint32_t *tile_of = reinterpret_cast<uint32_t *>(empty + kWsMaxStages);  // [kWsMaxStages]
+    uint64_t *full = reinterpret_cast<uint64_t *>(smem);   // [kWsMaxStages]
+    uint64_t *empty = full + kWsMaxStages;                  // [kWsMaxStages]
+    WsStageHeader *hdr = reinterpret_cast<WsStageHeader *>(smem + 2 * kWsMaxStages * 8);
     const uint32_t buf_bytes = a.max_slots * W * 4 + a.max_terms * uint32_t(sizeof(PlanTerm)) +
                                a.max_groups * uint32_t(sizeof(PlanGroup));
     const uint32_t terms_off = a.max_slots * W * 4;
     const uint32_t groups_off = terms_off + a.max_terms * uint32_t(sizeof(PlanTerm));
-    auto win_of = [&](uint32_t s) { return reinterpret_cast<uint32_t *>(smem + 128 + s * buf_bytes); };
-    auto terms_of = [&](uint32_t s) { return reinterpret_cast<PlanTerm *>(smem + 128 + s * buf_bytes + terms_off); };
+    auto win_of = [&](uint32_t s) { return reinterpret_cast<uint32_t *>(smem + kWsHeaderBytes + s * buf_bytes); };
+    auto terms_of = [&](uint32_t s) {
+        return reinterpret_cast<PlanTerm *>(smem + kWsHeaderBytes + s * buf_bytes + terms_off);
+    };
     auto groups_of = [&](uint32_t s) {
-        return reinterpret_cast<PlanGroup *>(smem + 128 + s * buf_bytes + groups_off);
+        return reinterpret_cast<PlanGroup *>(smem + kWsHeaderBytes + s * buf_bytes + groups_off);
     };
     const uint32_t warp = threadIdx.x / 32, lane = threadIdx.x % 32;
     if (threadIdx.x == 0) {
@@ -422,6 +437,9 @@ __global__ void __launch_bounds__(kWsThreads) k_score_ws(const ScoreArgs a) {
         // ------------------------------------------------------------ producer
         uint32_t pending = 0;  // stages with copies not yet consumed
         uint32_t it = 0;
+        uint32_t tile = 0;
+        if (lane == 0) tile = atomicAdd(a.tile_counter, 1u);
+        tile = __shfl_sync(0xFFFFFFFFu, tile, 0);
         for (;; ++it) {
             const uint32_t s = it % n_stages, round = it / n_stages;
             if (round > 0) {
@@ -431,18 +449,21 @@ __global__ void __launch_bounds__(kWsThreads) k_score_ws(const ScoreArgs a) {
                 if (!ok) break;
                 pending &= ~(1u << s);
             }
-            uint32_t tile = 0;
-            if (lane == 0) tile = atomicAdd(a.tile_counter, 1u);
-            tile = __shfl_sync(0xFFFFFFFFu, tile, 0);
-            if (lane == 0) tile_of[s] = tile;
             if (tile >= a.n_tiles) {
-                __syncwarp();
-                if (lane == 0) mbar_arrive(&full[s]);  // end-of-work marker
+                if (lane == 0) {
+                    hdr[s].tile = tile;
+                    mbar_arrive(&full[s]);  // end-of-work marker
+                }
                 return;
             }
             const PlanBlock blk = a.blocks[a.block_lo + tile % a.n_blocks];
             const uint32_t c0 = (tile / a.n_blocks) * W;
             const uint32_t valid = min(uint32_t(W), a.row_words - c0);
+            if (lane == 0) {
+                hdr[s].blk = blk;
+                hdr[s].tile = tile;
+                hdr[s].next_unit = 0;
+            }
             uint32_t *win = win_of(s);
             // rotated slots (NUM_REGIONS > 1): gathered by the producer lanes
             for (uint32_t sl_i = uint32_t(blk.n_slots) - blk.n_rot; sl_i < blk.n_slots; ++sl_i) {
@@ -450,11 +471,15 @@ __global__ void __launch_bounds__(kWsThreads) k_score_ws(const ScoreArgs a) {
                 if (sl.row - a.row_base >= a.n_rows) continue;
                 const uint32_t *src =
                     reinterpret_cast<const uint32_t *>(a.in + uint64_t(sl.row - a.row_base) * a.in_stride);
-                for (uint32_t x = lane; x < valid; x += 32) win[size_t(sl_i) * W + x] = rotated_word(src, c0 + x, sl.rot, a.N);
+                for (uint32_t x = lane; x < valid; x += 32)
+                    win[size_t(sl_i) * W + x] = rotated_word(src, c0 + x, sl.rot, a.N);
             }
             issue_tile_loads<W>(a, blk, c0, ((valid + 3u) & ~3u) * 4u, win, terms_of(s), groups_of(s), &full[s],
                                 lane);
             pending |= 1u << s;
+            // the next tile's index, fetched while this stage's copies fly
+            if (lane == 0) tile = atomicAdd(a.tile_counter, 1u);
+            tile = __shfl_sync(0xFFFFFFFFu, tile, 0);
         }
         // A wait expired: let every copy this CTA issued land before exiting.
         // The last n_stages iterations issued each stage's newest copies.
@@ -466,25 +491,40 @@ __global__ void __launch_bounds__(kWsThreads) k_score_ws(const ScoreArgs a) {
     }
 
     // --------------------------------------------------------------- consumers
-    const uint32_t ctid = threadIdx.x;  // 0 .. 32*kWsConsumers-1
-    const uint32_t team = ctid / TEAM, tlane = ctid % TEAM;
     for (uint32_t it = 0;; ++it) {
         const uint32_t s = it % n_stages, round = it / n_stages;
         if (!mbar_wait_bounded(&full[s], round & 1u, a.err)) return;
-        const uint32_t tile = tile_of[s];
+        const uint32_t tile = hdr[s].tile;
         if (tile >= a.n_tiles) return;
-        const PlanBlock blk = a.blocks[a.block_lo + tile % a.n_blocks];
+        const PlanBlock blk = hdr[s].blk;
         const uint32_t c0 = (tile / a.n_blocks) * W;
         const uint32_t valid = min(uint32_t(W), a.row_words - c0);
-        uint32_t bias_mask, zero_mask;
-        column_masks<Q, TEAM>(a, c0, tlane, bias_mask, zero_mask);
-        const uint32_t *wlane = win_of(s) + 4 * tlane;
+        uint32_t bmask[PARTS], zmask[PARTS];
+#pragma unroll
+        for (int p = 0; p < PARTS; ++p) column_masks<Q, TEAM>(a, c0, 32 * p + lane, bmask[p], zmask[p]);
         const PlanTerm *terms_s = terms_of(s);
         const PlanGroup *groups_s = groups_of(s);
-        for (uint32_t g = team; g < blk.n_groups; g += NTEAMS) {
+        const uint32_t n_units = blk.n_groups * PARTS;
+        uint32_t *next_unit = &hdr[s].next_unit;
+        uint32_t u = 0;
+        if (lane == 0) u = atomicAdd(next_unit, 1u);
+        u = __shfl_sync(0xFFFFFFFFu, u, 0);
+        while (u < n_units) {
+            uint32_t u_next = 0;  // taken now, its latency hides behind this unit
+            if (lane == 0) u_next = atomicAdd(next_unit, 1u);
+            const uint32_t g = u / PARTS, part = u % PARTS;
+            const uint32_t tlane = 32 * part + lane;
+            uint32_t bias_mask = bmask[0], zero_mask = zmask[0];
+#pragma unroll
+            for (int p = 1; p < PARTS; ++p)
+                if (part == uint32_t(p)) {
+                    bias_mask = bmask[p];
+                    zero_mask = zmask[p];
+                }
             const PlanGroup gr = groups_s[g];
             uint32_t acc[G][4 * Q];
             init_acc<G, Q>(acc, gr, bias_mask);
+            const uint32_t *wlane = win_of(s) + 4 * tlane;
             const PlanTerm *tp = terms_s + gr.term_begin;
 #pragma unroll 2
             for (uint32_t t = 0; t < gr.n_terms; ++t) {
@@ -496,6 +536,7 @@ __global__ void __launch_bounds__(kWsThreads) k_score_ws(const ScoreArgs a) {
                 mac<G, Q>(acc, tm, x);
             }
             write_outputs<G, Q, TEAM>(a, gr, acc, c0, tlane, valid, zero_mask);
+            u = __shfl_sync(0xFFFFFFFFu, u_next, 0);
         }
         __syncwarp();
         if (lane == 0) mbar_arrive(&empty[s]);
@@ -652,7 +693,7 @@ size_t kernel_smem_bytes(KernelKind kind, uint32_t slice_words, uint32_t max_slo
     switch (kind) {
         case KernelKind::kWindow: return 128 + buf;
         case KernelKind::kPipe: return 128 + 2 * buf;
-        case KernelKind::kWs: return 128 + size_t(n_stages) * buf;
+        case KernelKind::kWs: return kWsHeaderBytes + size_t(n_stages) * buf;
         default: return 0;
     }
 }

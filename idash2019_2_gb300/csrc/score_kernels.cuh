@@ -42,10 +42,12 @@ struct ScoreArgs {
 // kDirect: one CTA per tile, inputs read from global memory (plain form).
 // kPipe:   persistent, 512 threads, two buffers (next tile loads while the
 //          current one computes), one CTA per SM.
-// kWs:     persistent, warp-specialised: 1 producer + 8 consumer warps over a
-//          ring of n_stages buffers handed over with mbarriers.
+// kWs:     persistent, warp-specialised: one CTA of 1 producer + 15 consumer
+//          warps per SM over a ring of n_stages buffers handed over with
+//          mbarriers; consumers take (group, part) units from a shared counter.
 enum class KernelKind : int { kWindow = 0, kDirect = 1, kPipe = 2, kWs = 3 };
 constexpr uint32_t kMaxStages = 4;
+constexpr uint32_t kWsHeaderBytes = 512;  // kWs: barriers + per-stage headers before the ring
 
 // Slice widths the kernels are instantiated for.
 bool slice_supported(uint32_t slice_words);
