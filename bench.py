@@ -501,7 +501,10 @@ def run_ours(args):
     alg_bytes = info["algorithmic_in_rows"] * 8192 + model.n_out * 8192 + info["n_terms"] * 8 + model.n_out * 8
     peak, peak_src = peaks()
     achieved = alg_bytes / (ms_step / 1e3) / 1e9
-    traffic = profiled_traffic("trlwe_window_full.txt")
+    # DRAM bytes of one launch of the kernel kind the autotuner chose, from its
+    # ncu capture on this workload (null when that kind has none)
+    traffic = profiled_traffic({0: "trlwe_window_full.txt", 2: "trlwe_pipe_full.txt",
+                                3: "trlwe_ws_full.txt"}.get(info["kernel"], ""))
 
     # end to end through the host-memory entry point
     e2e_steps = max(3, min(args.steps, 20))
