@@ -90,9 +90,15 @@ __device__ __forceinline__ void init_acc(uint32_t (&acc)[G][4 * Q], const PlanGr
     }
 }
 
+template <int Q>
+__device__ __forceinline__ constexpr uint32_t all_columns() {
+    return (1u << (4 * Q)) - 1u;
+}
+
 template <int G, int Q, int TEAM>
 __device__ __forceinline__ void write_outputs(const ScoreArgs &a, const PlanGroup &gr, uint32_t (&acc)[G][4 * Q],
                                               uint32_t c0, uint32_t lane, uint32_t valid, uint32_t zero_mask) {
+    constexpr uint32_t W = 4 * Q * TEAM;
 #pragma unroll
     for (int m = 0; m < G; ++m) {
         const uint32_t o = gr.out[m];
@@ -104,6 +110,14 @@ __device__ __forceinline__ void write_outputs(const ScoreArgs &a, const PlanGrou
         }
         const uint64_t r = a.out_row_map ? uint64_t(a.out_row_map[o]) : uint64_t(o) - a.out_row_base;
         uint8_t *row = a.out + r * a.out_stride + uint64_t(c0) * 4;
+        if (valid >= W) {  // a full slice: every quad is inside the row
+#pragma unroll
+            for (int k = 0; k < Q; ++k)
+                stg_cs_v4(row + size_t(4 * lane + 4 * k * TEAM) * 4,
+                          make_int4(int(acc[m][4 * k]), int(acc[m][4 * k + 1]), int(acc[m][4 * k + 2]),
+                                    int(acc[m][4 * k + 3])));
+            continue;
+        }
 #pragma unroll
         for (int k = 0; k < Q; ++k) {
             const uint32_t q = 4 * lane + 4 * k * TEAM;
@@ -126,6 +140,63 @@ __device__ __forceinline__ void mac(uint32_t (&acc)[G][4 * Q], const PlanTerm &t
             acc[m][4 * k + 2] += c[m] * x[k].z;
             acc[m][4 * k + 3] += c[m] * x[k].w;
         }
+}
+
+// One group's accumulation over its terms from the shared-memory window
+// (wlane: the thread's first column in slot 0).  The first term initialises
+// the accumulators (IMAD with the bias as addend where the thread's columns
+// all take it), so no separate zeroing pass; a slice that crosses the edge of
+// the biased columns adds the bias per column afterwards (addition commutes
+// in Z/2^32).  Columns that the epilogue zeroes skip the arithmetic.
+template <int W, int G, int Q, int TEAM>
+__device__ __forceinline__ void accumulate_group(uint32_t (&acc)[G][4 * Q], const PlanGroup &gr,
+                                                 const PlanTerm *tp, const uint32_t *wlane, uint32_t bias_mask,
+                                                 uint32_t zero_mask) {
+    constexpr uint32_t kAll = all_columns<Q>();
+    const bool all_bias = bias_mask == kAll;
+    uint32_t b[G];
+#pragma unroll
+    for (int m = 0; m < G; ++m) b[m] = all_bias ? uint32_t(gr.bias[m]) : 0u;
+    if (gr.n_terms == 0 || zero_mask == kAll) {
+#pragma unroll
+        for (int m = 0; m < G; ++m)
+#pragma unroll
+            for (int e = 0; e < 4 * Q; ++e) acc[m][e] = b[m];
+    } else {
+        {
+            const PlanTerm tm = tp[0];
+            const uint32_t *w = wlane + size_t(tm.slot) * W;
+            uint4 x[Q];
+#pragma unroll
+            for (int k = 0; k < Q; ++k) x[k] = *reinterpret_cast<const uint4 *>(w + 4 * k * TEAM);
+            const uint32_t c[3] = {uint32_t(tm.c0), uint32_t(tm.c1), uint32_t(tm.c2)};
+#pragma unroll
+            for (int m = 0; m < G; ++m)
+#pragma unroll
+                for (int k = 0; k < Q; ++k) {
+                    acc[m][4 * k + 0] = b[m] + c[m] * x[k].x;
+                    acc[m][4 * k + 1] = b[m] + c[m] * x[k].y;
+                    acc[m][4 * k + 2] = b[m] + c[m] * x[k].z;
+                    acc[m][4 * k + 3] = b[m] + c[m] * x[k].w;
+                }
+        }
+#pragma unroll 2
+        for (uint32_t t = 1; t < gr.n_terms; ++t) {
+            const PlanTerm tm = tp[t];
+            const uint32_t *w = wlane + size_t(tm.slot) * W;
+            uint4 x[Q];
+#pragma unroll
+            for (int k = 0; k < Q; ++k) x[k] = *reinterpret_cast<const uint4 *>(w + 4 * k * TEAM);
+            mac<G, Q>(acc, tm, x);
+        }
+    }
+    if (bias_mask != 0 && !all_bias) {
+#pragma unroll
+        for (int m = 0; m < G; ++m)
+#pragma unroll
+            for (int e = 0; e < 4 * Q; ++e)
+                if (bias_mask & (1u << e)) acc[m][e] += uint32_t(gr.bias[m]);
+    }
 }
 
 // Value of column c (of the 2N-word TRLWE row) of X^(-m) * row:
@@ -225,17 +296,7 @@ __global__ void __launch_bounds__(kThreads) k_score_window(const ScoreArgs a) {
         for (uint32_t g = team; g < blk.n_groups; g += NTEAMS) {
             const PlanGroup gr = groups_s[g];
             uint32_t acc[G][4 * Q];
-            init_acc<G, Q>(acc, gr, bias_mask);
-            const PlanTerm *tp = terms_s + gr.term_begin;
-#pragma unroll 2
-            for (uint32_t t = 0; t < gr.n_terms; ++t) {
-                const PlanTerm tm = tp[t];
-                const uint32_t *w = wlane + size_t(tm.slot) * W;
-                uint4 x[Q];
-#pragma unroll
-                for (int k = 0; k < Q; ++k) x[k] = *reinterpret_cast<const uint4 *>(w + 4 * k * TEAM);
-                mac<G, Q>(acc, tm, x);
-            }
+            accumulate_group<W, G, Q, TEAM>(acc, gr, terms_s + gr.term_begin, wlane, bias_mask, zero_mask);
             write_outputs<G, Q, TEAM>(a, gr, acc, c0, lane, valid, zero_mask);
         }
         __syncthreads();
@@ -362,17 +423,7 @@ __global__ void __launch_bounds__(kPipeThreads, 1) k_score_pipe(const ScoreArgs 
         for (uint32_t g = team; g < blk.n_groups; g += NTEAMS) {
             const PlanGroup gr = groups_s[g];
             uint32_t acc[G][4 * Q];
-            init_acc<G, Q>(acc, gr, bias_mask);
-            const PlanTerm *tp = terms_s + gr.term_begin;
-#pragma unroll 2
-            for (uint32_t t = 0; t < gr.n_terms; ++t) {
-                const PlanTerm tm = tp[t];
-                const uint32_t *w = wlane + size_t(tm.slot) * W;
-                uint4 x[Q];
-#pragma unroll
-                for (int k = 0; k < Q; ++k) x[k] = *reinterpret_cast<const uint4 *>(w + 4 * k * TEAM);
-                mac<G, Q>(acc, tm, x);
-            }
+            accumulate_group<W, G, Q, TEAM>(acc, gr, terms_s + gr.term_begin, wlane, bias_mask, zero_mask);
             write_outputs<G, Q, TEAM>(a, gr, acc, c0, lane, valid, zero_mask);
         }
         cur = nxt;
@@ -523,18 +574,8 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_score_ws(const ScoreArgs a) {
                 }
             const PlanGroup gr = groups_s[g];
             uint32_t acc[G][4 * Q];
-            init_acc<G, Q>(acc, gr, bias_mask);
-            const uint32_t *wlane = win_of(s) + 4 * tlane;
-            const PlanTerm *tp = terms_s + gr.term_begin;
-#pragma unroll 2
-            for (uint32_t t = 0; t < gr.n_terms; ++t) {
-                const PlanTerm tm = tp[t];
-                const uint32_t *w = wlane + size_t(tm.slot) * W;
-                uint4 x[Q];
-#pragma unroll
-                for (int k = 0; k < Q; ++k) x[k] = *reinterpret_cast<const uint4 *>(w + 4 * k * TEAM);
-                mac<G, Q>(acc, tm, x);
-            }
+            accumulate_group<W, G, Q, TEAM>(acc, gr, terms_s + gr.term_begin, win_of(s) + 4 * tlane, bias_mask,
+                                            zero_mask);
             write_outputs<G, Q, TEAM>(a, gr, acc, c0, tlane, valid, zero_mask);
             u = __shfl_sync(0xFFFFFFFFu, u_next, 0);
         }
