@@ -83,6 +83,14 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t by
         : "memory");
 }
 
+// 16-byte shared-memory load at a 32-bit shared address.  Volatile: never
+// moved above the mbarrier wait that makes the data visible.
+__device__ __forceinline__ uint4 lds_v4(uint32_t addr) {
+    uint4 v;
+    asm volatile("ld.shared.v4.u32 {%0,%1,%2,%3}, [%4];" : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w) : "r"(addr));
+    return v;
+}
+
 __device__ __forceinline__ int4 ldg_nc_v4(const void *p) {
     int4 v;
     asm volatile("ld.global.nc.v4.s32 {%0,%1,%2,%3}, [%4];"

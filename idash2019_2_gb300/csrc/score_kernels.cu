@@ -163,13 +163,17 @@ __device__ __forceinline__ void accumulate_group(uint32_t (&acc)[G][4 * Q], cons
 #pragma unroll
             for (int e = 0; e < 4 * Q; ++e) acc[m][e] = b[m];
     } else {
+        // 32-bit shared addresses throughout: a term is {c0, c1, c2, slot},
+        // the slot's column slice starts slot * W words into the window.
+        const uint32_t wbase = smem_addr(wlane);
+        uint32_t taddr = smem_addr(tp);
         {
-            const PlanTerm tm = tp[0];
-            const uint32_t *w = wlane + size_t(tm.slot) * W;
+            const uint4 tv = lds_v4(taddr);
+            const uint32_t w = wbase + tv.w * (W * 4);
             uint4 x[Q];
 #pragma unroll
-            for (int k = 0; k < Q; ++k) x[k] = *reinterpret_cast<const uint4 *>(w + 4 * k * TEAM);
-            const uint32_t c[3] = {uint32_t(tm.c0), uint32_t(tm.c1), uint32_t(tm.c2)};
+            for (int k = 0; k < Q; ++k) x[k] = lds_v4(w + 16 * k * TEAM);
+            const uint32_t c[3] = {tv.x, tv.y, tv.z};
 #pragma unroll
             for (int m = 0; m < G; ++m)
 #pragma unroll
@@ -180,14 +184,24 @@ __device__ __forceinline__ void accumulate_group(uint32_t (&acc)[G][4 * Q], cons
                     acc[m][4 * k + 3] = b[m] + c[m] * x[k].w;
                 }
         }
+        const uint32_t tend = taddr + 16 * gr.n_terms;
 #pragma unroll 2
-        for (uint32_t t = 1; t < gr.n_terms; ++t) {
-            const PlanTerm tm = tp[t];
-            const uint32_t *w = wlane + size_t(tm.slot) * W;
+        for (taddr += 16; taddr != tend; taddr += 16) {
+            const uint4 tv = lds_v4(taddr);
+            const uint32_t w = wbase + tv.w * (W * 4);
             uint4 x[Q];
 #pragma unroll
-            for (int k = 0; k < Q; ++k) x[k] = *reinterpret_cast<const uint4 *>(w + 4 * k * TEAM);
-            mac<G, Q>(acc, tm, x);
+            for (int k = 0; k < Q; ++k) x[k] = lds_v4(w + 16 * k * TEAM);
+            const uint32_t c[3] = {tv.x, tv.y, tv.z};
+#pragma unroll
+            for (int m = 0; m < G; ++m)
+#pragma unroll
+                for (int k = 0; k < Q; ++k) {
+                    acc[m][4 * k + 0] += c[m] * x[k].x;
+                    acc[m][4 * k + 1] += c[m] * x[k].y;
+                    acc[m][4 * k + 2] += c[m] * x[k].z;
+                    acc[m][4 * k + 3] += c[m] * x[k].w;
+                }
         }
     }
     if (bias_mask != 0 && !all_bias) {
