@@ -257,6 +257,28 @@ def section_kinds(ctx, w, spec, d_in, d_out, steps):
     return out
 
 
+def section_decrypt(ctx, model, spec, d_out, seed, steps):
+    """Party A's decryption (decrypt_predictions, eval/idash.cpp:682-761) of
+    the headline's 242,646 output TRLWE: phase b - a*s at the 1,000 sample
+    coefficients, as float, device-resident (CUDA events)."""
+    from idash2019_2_gb300 import gpu
+    key = gpu.synth_key(seed)
+    ns = spec["num_samples"]
+    d_dec = ctx.device_alloc(model.n_out * ns * 4)
+    run = lambda: gpu.decrypt_device(ctx, key, d_out.ptr, gpu.DENSE_TRLWE, model.n_out, ns, d_dec.ptr)
+    for _ in range(3):
+        run()
+    ms = time_on_stream(ctx, run, steps)
+    d_dec.free()
+    nz = int(key.sum())
+    adds = model.n_out * ns * nz
+    return {"value": model.n_out * ns / (ms / 1e3), "unit": "decrypted scores/s", "ms_per_step": ms,
+            "rows": model.n_out, "samples": ns, "key_weight": nz,
+            "word_adds_per_s": adds / (ms / 1e3),
+            "kernel": "k_decrypt_phase: one CTA per row, negacyclic extension of the mask in shared memory, "
+                      "4 coefficients per thread over the key's nonzero positions"}
+
+
 def section_lwe(ctx, name, seed, n_indiv, n_tags, n_targets, neighbours=5, choices=None, passes=2, chunk=2048):
     """Per-individual LWE form: inputs resident (n_indiv LWE samples of n=1024
     per feature row), outputs produced range by range into a 2-slot HBM ring
@@ -543,11 +565,13 @@ def run_ours(args):
         forms["plain"]["batched_over_plain"] = value / forms["plain"]["value"]
     if world == 1 and "kinds" in sections:
         forms["kinds"] = section_kinds(ctx, w, spec, d_in, d_out, min(args.steps, 200))
+    if world == 1 and "decrypt" in sections:
+        forms["decrypt"] = section_decrypt(ctx, model, spec, d_out, args.seed + rank, min(args.steps, 50))
     d_in.free()
     d_out.free()
     model.free()
     if world == 1:
-        forms.update(run_sections(ctx, args, sections - {"plain", "kinds"}))
+        forms.update(run_sections(ctx, args, sections - {"plain", "kinds", "decrypt"}))
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -579,7 +603,7 @@ def main():
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="trlwe_full")
     ap.add_argument("--seed", type=int, default=0x1DA52019)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--sections", default="plain,lwe_full,batched_uneven,intpoly,serving",
+    ap.add_argument("--sections", default="plain,kinds,decrypt,lwe_full,batched_uneven,intpoly,serving",
                     help="extra forms measured after the headline (comma list, '' for none)")
     ap.add_argument("--no-headline", action="store_true",
                     help="measure only --sections (no headline, e2e or CPU baseline)")

@@ -101,6 +101,11 @@ class CloudReport(C.Structure):
                 ("model_from_cache", C.c_uint32), ("reserved", C.c_uint32)]
 
 
+class DecryptReport(C.Structure):
+    _fields_ = [("read_s", C.c_double), ("decrypt_s", C.c_double), ("write_s", C.c_double),
+                ("n_records", C.c_uint64), ("n_lines", C.c_uint64)]
+
+
 # name -> (restype, argtypes); every function include/idash_gpu.h declares.
 PROTOTYPES = {
     "idash_status_string": (C.c_char_p, [status_t]),
@@ -148,6 +153,11 @@ PROTOTYPES = {
                                              vp, C.POINTER(RowLayout), vp, C.POINTER(RowLayout), vp]),
     "idash_cloud_files": (status_t, [C.c_int, C.c_char_p, C.c_char_p, C.c_char_p, C.c_char_p,
                                      C.POINTER(CloudReport), C.c_char_p, C.c_size_t]),
+    "idash_decrypt_trlwe_device": (status_t, [vp, i32p, C.c_uint32, vp, C.POINTER(RowLayout), C.c_uint64,
+                                              C.c_uint32, vp, vp]),
+    "idash_decrypt_files": (status_t, [C.c_int, C.c_char_p, C.c_char_p, C.c_char_p, C.c_int,
+                                       C.POINTER(DecryptReport), C.c_char_p, C.c_size_t]),
+    "idash_synth_key": (None, [C.c_uint64, C.c_uint32, i32p]),
     "idash_synth_model": (status_t, [C.POINTER(SynthSpec), C.POINTER(SynthModel)]),
     "idash_synth_model_free": (None, [C.POINTER(SynthModel)]),
     "idash_synth_lwe_device": (status_t, [vp, C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint64, vp, C.c_uint64,

@@ -5,6 +5,7 @@ translation unit, in parallel) and links, inside the package directory:
 
   libidash_gpu.so   the C ABI declared in include/idash_gpu.h
   idash_cloud       the cloud CLI (eval/cloud.cpp's argv and output)
+  idash_decrypt     the decryption CLI (eval/decrypt.cpp's argv and output)
 
 Objects go to idash2019_2_gb300/_build/ (git-ignored).
 """
@@ -22,6 +23,7 @@ CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libidash_gpu.so")
 CLI = os.path.join(PKG, "idash_cloud")
+DECRYPT_CLI = os.path.join(PKG, "idash_decrypt")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O3",
@@ -35,9 +37,11 @@ LIB_SOURCES = [
     "csrc/server.cpp",
     "csrc/capi.cpp",
     "csrc/plan.cpp",
+    "csrc/decrypt.cu",
     "csrc/host/idash_host.cpp",
+    "csrc/host/decrypt_host.cpp",
 ]
-CLI_SOURCES = ["csrc/host/cloud_main.cpp"]
+CLIS = {CLI: ["csrc/host/cloud_main.cpp"], DECRYPT_CLI: ["csrc/host/decrypt_main.cpp"]}
 
 
 def _nvcc() -> str:
@@ -83,7 +87,7 @@ def _compile(nvcc: str, src: str, verbose: bool) -> str:
 def build(verbose: bool = False) -> None:
     nvcc = _nvcc()
     os.makedirs(BUILD, exist_ok=True)
-    srcs = LIB_SOURCES + CLI_SOURCES
+    srcs = LIB_SOURCES + [s for v in CLIS.values() for s in v]
     with cf.ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 2)) as ex:
         objs = dict(zip(srcs, ex.map(lambda s: _compile(nvcc, s, verbose), srcs)))
     lib_objs = [objs[s] for s in LIB_SOURCES]
@@ -92,12 +96,13 @@ def build(verbose: bool = False) -> None:
         if verbose:
             print(" ".join(cmd), flush=True)
         subprocess.run(cmd, check=True)
-    cli_objs = lib_objs + [objs[s] for s in CLI_SOURCES]
-    if _deps_newer(CLI, cli_objs):
-        cmd = [nvcc, *ARCH, "-o", CLI, *cli_objs, "-cudart", "static"]
-        if verbose:
-            print(" ".join(cmd), flush=True)
-        subprocess.run(cmd, check=True)
+    for exe, main_srcs in CLIS.items():
+        exe_objs = lib_objs + [objs[s] for s in main_srcs]
+        if _deps_newer(exe, exe_objs):
+            cmd = [nvcc, *ARCH, "-o", exe, *exe_objs, "-cudart", "static"]
+            if verbose:
+                print(" ".join(cmd), flush=True)
+            subprocess.run(cmd, check=True)
 
 
 if __name__ == "__main__":

@@ -420,6 +420,7 @@ void idash_close(idash_ctx *ctx) {
     cudaFree(ctx->d_counters);
     cudaFree(ctx->d_in_buf);
     cudaFree(ctx->d_out_buf);
+    cudaFree(ctx->d_key_buf);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     if (ctx->h2d) cudaStreamDestroy(ctx->h2d);
     if (ctx->d2h) cudaStreamDestroy(ctx->d2h);

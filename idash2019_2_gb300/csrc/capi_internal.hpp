@@ -59,6 +59,8 @@ struct idash_ctx {
     // buffers for the host-memory path (grow only)
     uint8_t *d_in_buf = nullptr, *d_out_buf = nullptr;
     size_t d_in_cap = 0, d_out_cap = 0;
+    void *d_key_buf = nullptr;  // decryption key's nonzero positions and values (grow only)
+    size_t d_key_cap = 0;
     std::vector<cudaEvent_t> events;
 
     idash_status fail(idash_status s, const std::string &msg) {

@@ -1,0 +1,134 @@
+// Party A's decryption of the output TRLWE on the GPU: decrypt_predictions
+// (eval/idash.cpp:682-761) computes, per output ciphertext, the phase
+// b - a*s (tLwePhase: a negacyclic polynomial product mod X^N + 1 over
+// Z/2^32 with the integer key s) and reads its coefficients
+// [0, NUM_SAMPLES) as t32tod(phase[j]) = phase[j] / 2^32, stored as float.
+//
+// The product is exact: only the key's nonzero coefficients are visited (a
+// TFHE key is binary, so about N/2 of them), and each of the NUM_SAMPLES
+// coefficients is a sum of N/2 words mod 2^32.  The float conversion
+// float(phase / 2^32) equals float(phase) * 2^-32 exactly (scaling by a power
+// of two commutes with round-to-nearest for these magnitudes).
+#include <algorithm>
+#include <vector>
+
+#include "capi_internal.hpp"
+#include "common.cuh"
+
+namespace idash {
+namespace {
+
+constexpr uint32_t kDecryptThreads = 256;
+constexpr uint32_t kDecryptCols = 4;  // consecutive coefficients per thread
+
+// One CTA per row (grid-stride over rows).  Shared memory: ext[2N], the
+// negacyclic extension of the mask a (ext[N + t] = a[t], ext[t] = -a[t]) so
+// that (a*s)[j] = sum_i s_i * ext[N + j - i]; then the key's nonzero
+// positions (and values, for a non-binary key).
+template <bool kBinary>
+__global__ void __launch_bounds__(kDecryptThreads) k_decrypt_phase(const uint8_t *in, uint64_t in_stride,
+                                                                   uint32_t N, uint32_t num_samples,
+                                                                   const uint32_t *key_idx, const int32_t *key_val,
+                                                                   uint32_t n_nz, uint64_t n_rows, float *out) {
+    extern __shared__ __align__(16) uint32_t sh[];
+    uint32_t *ext = sh;
+    uint32_t *idx = sh + 2 * N;
+    int32_t *val = reinterpret_cast<int32_t *>(idx + n_nz);
+    for (uint32_t q = threadIdx.x; q < n_nz; q += blockDim.x) {
+        idx[q] = key_idx[q];
+        if (!kBinary) val[q] = key_val[q];
+    }
+    for (uint64_t row = blockIdx.x; row < n_rows; row += gridDim.x) {
+        const uint32_t *a = reinterpret_cast<const uint32_t *>(in + row * in_stride);
+        __syncthreads();  // the previous row is done with ext
+        for (uint32_t t = threadIdx.x; t < N; t += blockDim.x) {
+            const uint32_t v = a[t];
+            ext[N + t] = v;
+            ext[t] = 0u - v;
+        }
+        __syncthreads();
+        for (uint32_t j0 = threadIdx.x * kDecryptCols; j0 < num_samples; j0 += blockDim.x * kDecryptCols) {
+            uint32_t acc[kDecryptCols];
+#pragma unroll
+            for (uint32_t r = 0; r < kDecryptCols; ++r) acc[r] = 0;
+            // j0 is a multiple of 4 below N (a power of two >= 4), so j0 + r < N
+            // and ext[N + j0 + r - i] stays inside [1, 2N) for every i < N
+            const uint32_t *e = ext + N + j0;
+#pragma unroll 4
+            for (uint32_t q = 0; q < n_nz; ++q) {
+                const uint32_t *p = e - idx[q];
+                const uint32_t s = kBinary ? 1u : uint32_t(val[q]);
+#pragma unroll
+                for (uint32_t r = 0; r < kDecryptCols; ++r) acc[r] += kBinary ? p[r] : s * p[r];
+            }
+#pragma unroll
+            for (uint32_t r = 0; r < kDecryptCols; ++r) {
+                const uint32_t j = j0 + r;
+                if (j < num_samples) {
+                    const uint32_t phase = a[N + j] - acc[r];
+                    out[row * num_samples + j] = __int2float_rn(int32_t(phase)) * 0x1p-32f;
+                }
+            }
+        }
+    }
+}
+
+}  // namespace
+}  // namespace idash
+
+using namespace idash;
+
+extern "C" idash_status idash_decrypt_trlwe_device(idash_ctx *ctx, const int32_t *key, uint32_t N, const void *d_in,
+                                                   const idash_row_layout *in_layout, uint64_t n_rows,
+                                                   uint32_t num_samples, float *d_out, void *stream) {
+    if (!ctx) return IDASH_ERR_INVALID_ARGUMENT;
+    if (!key || !d_in || !in_layout || !d_out || N < 4 || N > 4096 || (N & (N - 1)) || num_samples == 0 ||
+        num_samples > N)
+        return ctx->fail(IDASH_ERR_INVALID_ARGUMENT, "idash_decrypt_trlwe_device: bad arguments");
+    if (in_layout->row_stride < uint64_t(2) * N * 4 || in_layout->payload_offset % 4 || in_layout->row_stride % 4)
+        return ctx->fail(IDASH_ERR_INVALID_ARGUMENT, "idash_decrypt_trlwe_device: bad row layout");
+    if (n_rows == 0) return IDASH_OK;
+    std::vector<uint32_t> idx;
+    std::vector<int32_t> val;
+    bool binary = true;
+    for (uint32_t i = 0; i < N; ++i)
+        if (key[i] != 0) {
+            idx.push_back(i);
+            val.push_back(key[i]);
+            binary = binary && key[i] == 1;
+        }
+    cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+    const size_t key_bytes = std::max<size_t>(idx.size(), 1) * 8;
+    if (ctx->d_key_cap < key_bytes) {
+        cudaFree(ctx->d_key_buf);
+        ctx->d_key_buf = nullptr;
+        ctx->d_key_cap = 0;
+        idash_status st = ctx->check_cuda(cudaMalloc(&ctx->d_key_buf, key_bytes), "cudaMalloc key");
+        if (st != IDASH_OK) return st;
+        ctx->d_key_cap = key_bytes;
+    }
+    uint32_t *d_idx = static_cast<uint32_t *>(ctx->d_key_buf);
+    int32_t *d_val = reinterpret_cast<int32_t *>(d_idx + std::max<size_t>(idx.size(), 1));
+    if (!idx.empty()) {
+        // pageable source: the call returns once the bytes are staged
+        idash_status st = ctx->check_cuda(
+            cudaMemcpyAsync(d_idx, idx.data(), idx.size() * 4, cudaMemcpyHostToDevice, s), "key upload");
+        if (st == IDASH_OK)
+            st = ctx->check_cuda(cudaMemcpyAsync(d_val, val.data(), val.size() * 4, cudaMemcpyHostToDevice, s),
+                                 "key upload");
+        if (st != IDASH_OK) return st;
+    }
+    const uint32_t n_nz = uint32_t(idx.size());
+    const size_t smem = size_t(2) * N * 4 + size_t(n_nz) * (binary ? 4 : 8);
+    const uint32_t blocks = uint32_t(std::min<uint64_t>(n_rows, uint64_t(ctx->sm_count) * 8));
+    const uint8_t *in = static_cast<const uint8_t *>(d_in) + in_layout->payload_offset;
+    if (binary)
+        k_decrypt_phase<true><<<blocks, kDecryptThreads, smem, s>>>(in, in_layout->row_stride, N, num_samples, d_idx,
+                                                                   d_val, n_nz, n_rows, d_out);
+    else
+        k_decrypt_phase<false><<<blocks, kDecryptThreads, smem, s>>>(in, in_layout->row_stride, N, num_samples,
+                                                                    d_idx, d_val, n_nz, n_rows, d_out);
+    idash_status st = ctx->check_cuda(cudaGetLastError(), "k_decrypt_phase launch");
+    if (st == IDASH_OK) ctx->stats.kernel_launches++;
+    return st;
+}

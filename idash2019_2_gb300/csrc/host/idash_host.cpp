@@ -93,6 +93,10 @@ idash_status RecordImage::allocate(uint64_t n) {
 Status read_params(IdashParams &params, const std::string &filename) {
     std::ifstream in(filename, std::ios::binary);
     if (!in) return Status::Err(IDASH_ERR_IO, "cannot open parameters file '" + filename + "'");
+    return read_params_stream(params, in);
+}
+
+Status read_params_stream(IdashParams &params, std::istream &in) {
     uint32_t hdr[7];
     if (!read_exact(in, hdr, sizeof(hdr))) return Status::Err(IDASH_ERR_FORMAT, "params.bin: truncated header");
     params = IdashParams();

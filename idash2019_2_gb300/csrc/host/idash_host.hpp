@@ -7,6 +7,7 @@
 
 #include <array>
 #include <cstdint>
+#include <iosfwd>
 #include <string>
 #include <unordered_map>
 #include <utility>
@@ -81,6 +82,7 @@ struct Status {
 
 // params.bin (eval/idash.cpp:128-186, 200-261).
 Status read_params(IdashParams &params, const std::string &filename);
+Status read_params_stream(IdashParams &params, std::istream &in);  // read_params_istream
 Status write_params(const IdashParams &params, const std::string &filename);
 // <dir>/<pos>_<snp>.hr for every output position (eval/idash.cpp:66-114,
 // eval/parse_vw.cpp:8-30).
@@ -130,5 +132,36 @@ Status cloud_compute_score(EncryptedPredictions &preds, const EncryptedData &dat
 // parsed and, when cache_path is non-empty, cached there).
 Status load_model(Model *parsed, FlatModel *flat, const IdashParams &params, const std::string &params_file,
                   const std::string &model_dir, const std::string &cache_path, bool *from_cache);
+
+// ------------------------------------------------------------ decryption
+// keys.bin (write_key / read_key, eval/idash.cpp:476-502): the params.bin
+// content, then the TRLWE key record (int32 tag, int32 N, int32 k,
+// double alpha_min, double alpha_max, k * N int32 coefficients).
+struct IdashKey {
+    IdashParams params;
+    uint32_t N = 0, k = 0;
+    double alpha_min = 0, alpha_max = 0;
+    std::vector<int32_t> key;  // k * N coefficients
+};
+constexpr int32_t kTlweKeyTag = 52;  // record tag of the key stream format
+Status read_key(IdashKey &key, const std::string &filename);
+
+// eval/idash.h:190-211, held as one matrix: the scores of the prediction
+// file's record r at [r * num_samples, (r + 1) * num_samples).
+struct DecryptedPredictions {
+    uint32_t num_samples = 0;
+    std::vector<float> scores;
+    std::unordered_map<FeatBigIndex, uint64_t> row_of;  // FeatBigIndex -> record
+};
+// Every output the params name has a record in the predictions.
+Status check_predictions(const EncryptedPredictions &preds, const IdashParams &params);
+// decrypt_predictions (eval/idash.cpp:682-761): every record's phase on the
+// GPU, t32tod of coefficients [0, NUM_SAMPLES) as float.
+Status decrypt_predictions(DecryptedPredictions &dec, const EncryptedPredictions &preds, const IdashKey &key,
+                           idash_ctx *ctx);
+// write_decrypted_predictions (eval/idash.cpp:436-469), byte for byte;
+// formatted on all host threads.
+Status write_decrypted_predictions(const DecryptedPredictions &dec, const IdashParams &params,
+                                   const std::string &filename, bool print_pos_name, uint64_t *n_lines = nullptr);
 
 }  // namespace idash_host

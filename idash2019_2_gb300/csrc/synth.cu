@@ -306,6 +306,10 @@ extern "C" idash_status idash_synth_trlwe_device(idash_ctx *ctx, uint64_t seed, 
                            "k_synth_trlwe launch");
 }
 
+extern "C" void idash_synth_key(uint64_t seed, uint32_t N, int32_t *out) {
+    if (!out) return;
+    for (uint32_t j = 0; j < N; ++j) out[j] = int32_t(hash32(seed, 1, j) & 1u);
+}
 
 extern "C" idash_status idash_synth_uniform_device(idash_ctx *ctx, uint64_t seed, uint64_t row_begin, uint64_t n_rows,
                                                    uint32_t row_words, void *d_out, uint64_t row_stride,

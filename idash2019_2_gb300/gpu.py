@@ -429,3 +429,33 @@ def cloud_files(params_file: str, model_dir: str, data_file: str, pred_file: str
     if code != 0:
         raise IdashError(code, err.value.decode(errors="replace"))
     return {k: getattr(rep, k) for k, _ in rep._fields_}
+
+
+def decrypt_device(ctx: Context, key: np.ndarray, d_in: int, layout: RowLayout, n_rows: int, num_samples: int,
+                   d_out: int, stream=None):
+    """Phase b - a*s of n_rows TRLWE rows at coefficients [0, num_samples),
+    as float t32tod (idash_decrypt_trlwe_device); d_out: n_rows x num_samples
+    float32."""
+    key = np.ascontiguousarray(key, np.int32)
+    ctx.check(ctx.lib.idash_decrypt_trlwe_device(ctx.h, _p(key, C.c_int32), len(key), C.c_void_p(d_in),
+                                                 C.byref(layout), n_rows, num_samples, C.c_void_p(d_out),
+                                                 C.c_void_p(stream) if stream else None))
+
+
+def decrypt_files(keys_file: str, pred_file: str, csv_file: str, by_position: bool, device: int = 0) -> dict:
+    """eval/decrypt.cpp's flow on files (idash_decrypt_files)."""
+    lib = _lib.load()
+    rep = _lib.DecryptReport()
+    err = C.create_string_buffer(1024)
+    code = lib.idash_decrypt_files(device, keys_file.encode(), pred_file.encode(), csv_file.encode(),
+                                   1 if by_position else 0, C.byref(rep), err, len(err))
+    if code != 0:
+        raise IdashError(code, err.value.decode(errors="replace"))
+    return {k: getattr(rep, k) for k, _ in rep._fields_}
+
+
+def synth_key(seed: int, N: int = 1024) -> np.ndarray:
+    """The binary key the synthetic generators encrypt under."""
+    out = np.zeros(N, np.int32)
+    _lib.load().idash_synth_key(seed, N, _p(out, C.c_int32))
+    return out

@@ -314,6 +314,37 @@ typedef struct {
 idash_status idash_cloud_files(int device, const char *params_file, const char *model_dir, const char *data_file,
                                const char *pred_file, idash_cloud_report *report, char *errbuf, size_t errbuf_len);
 
+/* ------------------------------------------- decryption (party A)
+ * decrypt_predictions (eval/idash.cpp:682-761) on the device: for each of
+ * n_rows TRLWE rows (k = 1, layout in_layout), the phase b - a*s (tLwePhase,
+ * an exact negacyclic product mod X^N + 1 over Z/2^32 with the integer key s)
+ * at coefficients [0, num_samples), converted as t32tod to float:
+ * d_out[r * num_samples + j] = float(phase_r[j] / 2^32).  key: the key's N
+ * integer coefficients in host memory (binary for TFHE keys; any integers
+ * are accepted).  N a power of two in [4, 4096].  Asynchronous on `stream`
+ * once the key has been staged (the call synchronises with `stream` first). */
+idash_status idash_decrypt_trlwe_device(idash_ctx *ctx, const int32_t *key, uint32_t N, const void *d_in,
+                                        const idash_row_layout *in_layout, uint64_t n_rows, uint32_t num_samples,
+                                        float *d_out, void *stream);
+
+/* eval/decrypt.cpp:13-48 as one call: reads keys.bin (read_key,
+ * eval/idash.cpp:488-502: params.bin's content followed by the key record)
+ * and encrypted_prediction.bin, decrypts on `device`, and writes the CSV of
+ * write_decrypted_predictions (eval/idash.cpp:436-469) byte for byte: header
+ * "Subject ID,target SNP,0,1,2", then one line per (sample, output position)
+ * with the position's name (by_position = 0) or number (by_position = 1) and
+ * the three scores printed as an iostream prints a float (6 significant
+ * digits).  Key record: int32 tag, int32 N, int32 k, double alpha_min,
+ * double alpha_max, k * N int32 coefficients. */
+typedef struct {
+    double read_s;     /* key + prediction file reads */
+    double decrypt_s;  /* host->device copy, phase kernel, device->host copy */
+    double write_s;    /* CSV formatting and write */
+    uint64_t n_records, n_lines;
+} idash_decrypt_report;
+idash_status idash_decrypt_files(int device, const char *keys_file, const char *pred_file, const char *csv_file,
+                                 int by_position, idash_decrypt_report *report, char *errbuf, size_t errbuf_len);
+
 /* ------------------------------------------- synthetic workloads (host)
  * Seeded synthetic imputation models with the reference's shapes: tag SNPs at
  * sorted positions, targets at sorted random positions, each target's
@@ -351,6 +382,8 @@ idash_status idash_synth_lwe_device(idash_ctx *ctx, uint64_t seed, uint32_t n, u
                                     uint64_t n_feat_rows, int32_t *d_out, uint64_t row_stride, void *stream);
 idash_status idash_synth_trlwe_device(idash_ctx *ctx, uint64_t seed, const idash_trlwe_params *params,
                                       uint32_t n_tags, void *d_out, const idash_row_layout *layout, void *stream);
+/* The binary key those generators encrypt under: N coefficients in {0, 1}. */
+void idash_synth_key(uint64_t seed, uint32_t N, int32_t *out);
 /* Uniformly random ciphertext rows (statistically the same as encryptions):
  * word j of global row r = hash(seed, r * row_words + j); rows
  * [row_begin, row_begin + n_rows) are written from d_out on. */

@@ -172,6 +172,26 @@ void oracle_sample_extract(uint32_t N, const int32_t *trlwe, uint32_t slot, int3
     out[N] = trlwe[N + slot];
 }
 
+void oracle_trlwe_decrypt(uint32_t N, const int32_t *key, uint64_t n_rows, uint64_t stride_words,
+                          const int32_t *rows, uint32_t num_samples, float *out, int n_threads) {
+#pragma omp parallel for num_threads(n_threads > 0 ? n_threads : 1) schedule(dynamic, 16)
+    for (int64_t r = 0; r < (int64_t)n_rows; ++r) {
+        const uint32_t *a = (const uint32_t *)(rows + (uint64_t)r * stride_words);
+        const uint32_t *b = a + N;
+        for (uint32_t j = 0; j < num_samples; ++j) {
+            /* (a*s)[j] = sum_{i<=j} s_i a_{j-i} - sum_{i>j} s_i a_{N+j-i} */
+            uint32_t acc = 0;
+            for (uint32_t i = 0; i < N; ++i) {
+                const uint32_t s = (uint32_t)key[i];
+                if (s == 0) continue;
+                acc += i <= j ? s * a[j - i] : 0u - s * a[N + j - i];
+            }
+            const int32_t phase = (int32_t)(b[j] - acc);
+            out[(uint64_t)r * num_samples + j] = (float)((double)phase / 4294967296.0);
+        }
+    }
+}
+
 /* Synthetic per-individual LWE inputs (streams as in the product generator):
  *   key bit s_j      = hash(seed, 1, j) & 1
  *   genotype g(p,i)  = hash(seed, 2, p*n_indiv + i) % 3, feature f = 3p+v has bit (g == v)

@@ -74,6 +74,14 @@ int oracle_intpoly_score(uint32_t N, uint32_t num_samples, uint32_t region_size,
  * -a[N+s-j] (j>s); b' = b[s].  out has N+1 words. */
 void oracle_sample_extract(uint32_t N, const int32_t *trlwe, uint32_t slot, int32_t *out);
 
+/* Party A's decryption of TRLWE rows (decrypt_predictions,
+ * eval/idash.cpp:682-761): phase = b - a*s (tLwePhase, eval/idash.cpp:714,
+ * exact negacyclic product mod X^N+1 over Z/2^32 with the integer key s),
+ * then out[r*num_samples + j] = (float)t32tod(phase[j]) (:718) for
+ * j < num_samples.  rows: [n_rows][stride_words] int32, a at word 0, b at N. */
+void oracle_trlwe_decrypt(uint32_t N, const int32_t *key, uint64_t n_rows, uint64_t stride_words,
+                          const int32_t *rows, uint32_t num_samples, float *out, int n_threads);
+
 /* Counter-based generator shared with the product's synthetic-workload
  * generator: splitmix64 finaliser over (seed, stream, index). */
 uint64_t oracle_mix64(uint64_t z);

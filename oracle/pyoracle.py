@@ -47,6 +47,9 @@ def lib() -> C.CDLL:
                                            i16p, i32p, C.c_uint64, i32p, C.c_uint64, C.c_uint64, i32p, C.c_int]
         L.oracle_sample_extract.argtypes = [C.c_uint32, i32p, C.c_uint32, i32p]
         L.oracle_sample_extract.restype = None
+        L.oracle_trlwe_decrypt.argtypes = [C.c_uint32, i32p, C.c_uint64, C.c_uint64, i32p, C.c_uint32,
+                                           C.POINTER(C.c_float), C.c_int]
+        L.oracle_trlwe_decrypt.restype = None
         L.oracle_hash32.argtypes = [C.c_uint64, C.c_uint64, C.c_uint64]
         L.oracle_hash32.restype = C.c_uint32
         L.oracle_synth_lwe_words.argtypes = [C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint64, C.c_uint64,
@@ -120,6 +123,18 @@ def sample_extract(trlwe_row: np.ndarray, slot: int) -> np.ndarray:
     row = np.ascontiguousarray(trlwe_row, np.int32)
     out = np.zeros(len(row) // 2 + 1, np.int32)
     lib().oracle_sample_extract(len(row) // 2, _p(row, C.c_int32), slot, _p(out, C.c_int32))
+    return out
+
+
+def trlwe_decrypt(rows: np.ndarray, key: np.ndarray, num_samples: int, n_threads: int = 0) -> np.ndarray:
+    """Phase b - a*s of each TRLWE row at coefficients [0, num_samples) as
+    float t32tod (decrypt_predictions, eval/idash.cpp:682-761); rows are
+    [n][stride] int32 with a at word 0 and b at word N."""
+    rows = np.ascontiguousarray(rows, np.int32)
+    key = np.ascontiguousarray(key, np.int32)
+    out = np.zeros((rows.shape[0], num_samples), np.float32)
+    lib().oracle_trlwe_decrypt(len(key), _p(key, C.c_int32), rows.shape[0], rows.shape[1], _p(rows, C.c_int32),
+                               num_samples, out.ctypes.data_as(C.POINTER(C.c_float)), n_threads or os.cpu_count())
     return out
 
 

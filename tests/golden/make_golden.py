@@ -78,14 +78,27 @@ def make_small(name, n_indiv, n_tags, n_targets, neighbours, nan_rate, edits, se
         run([os.path.join(REF_BIN, "encrypt"), "tags.txt"], d, env)
         run([os.path.join(REF_BIN, "cloud1"), "model"], d, env)
         run([os.path.join(REF_BIN, "decrypt"), "bypos"], d, env)
+        run([os.path.join(REF_BIN, "decrypt")], d, env)
         if os.path.exists(out):
             shutil.rmtree(out)
         os.makedirs(out)
         for f in ["params.bin", "keys.bin", "encrypted_data.bin", "encrypted_prediction.bin", "result_bypos.csv",
-                  "tags.txt", "targets.txt"]:
+                  "result.csv", "tags.txt", "targets.txt"]:
             shutil.copy(os.path.join(d, f), os.path.join(out, f))
         shutil.copytree(os.path.join(d, "model"), os.path.join(out, "model"))
     print(f"{name}: {sorted(os.listdir(out))}")
+
+
+def add_named_csv(name):
+    """The reference's decrypt without arguments (result.csv, target SNPs by
+    name) on a committed case's keys and predictions."""
+    out = os.path.join(HERE, name)
+    with tempfile.TemporaryDirectory() as d:
+        for f in ["keys.bin", "encrypted_prediction.bin"]:
+            shutil.copy(os.path.join(out, f), os.path.join(d, f))
+        run([os.path.join(REF_BIN, "decrypt")], d)
+        shutil.copy(os.path.join(d, "result.csv"), os.path.join(out, "result.csv"))
+    print(f"{name}: result.csv")
 
 
 def make_hashed():
@@ -104,6 +117,10 @@ def make_hashed():
 def main():
     ref = os.environ.get("REF_DIR", "/root/reference")
     run(["make", "-s", "ref", f"REF_DIR={ref}"], os.path.join(ROOT, "oracle"))
+    if "--named-csv" in sys.argv:  # only add result.csv to the committed cases
+        for name in SMALL_CASES:
+            add_named_csv(name)
+        return
     for i, (name, args) in enumerate(SMALL_CASES.items()):
         make_small(name, *args, seed=100 + i)
     make_hashed()

@@ -80,3 +80,55 @@ def test_truncated_ciphertexts(case):
 
 def test_missing_ciphertexts(case):
     expect(case, "IDASH_ERR_IO", data="absent.bin")
+
+
+# ------------------------------------------------ decryption inputs (party A)
+@pytest.fixture()
+def dcase(tmp_path):
+    try:
+        gpu._lib.load()
+    except ImportError as e:
+        pytest.skip(str(e))
+    src = os.path.join(GOLDEN, "ref_r10")
+    for f in ["keys.bin", "encrypted_prediction.bin"]:
+        shutil.copy(os.path.join(src, f), tmp_path / f)
+    return tmp_path
+
+
+def dexpect(d, name, keys="keys.bin", preds="encrypted_prediction.bin"):
+    with pytest.raises(gpu.IdashError) as e:
+        gpu.decrypt_files(str(d / keys), str(d / preds), str(d / "out.csv"), True, device=0)
+    assert e.value.name == name, str(e.value)
+    assert not (d / "out.csv").exists()
+    return str(e.value)
+
+
+def test_decrypt_missing_key(dcase):
+    assert "nope.bin" in dexpect(dcase, "IDASH_ERR_IO", keys="nope.bin")
+
+
+def test_decrypt_truncated_key(dcase):
+    raw = (dcase / "keys.bin").read_bytes()
+    (dcase / "keys.bin").write_bytes(raw[:-100])
+    assert "truncated" in dexpect(dcase, "IDASH_ERR_FORMAT")
+
+
+def test_decrypt_key_record_tag(dcase):
+    raw = bytearray((dcase / "keys.bin").read_bytes())
+    raw[len(raw) - (12 + 16 + 4096)] ^= 0xFF  # the key record's tag
+    (dcase / "keys.bin").write_bytes(bytes(raw))
+    assert "key record" in dexpect(dcase, "IDASH_ERR_FORMAT")
+
+
+def test_decrypt_missing_prediction_record(dcase):
+    raw = (dcase / "encrypted_prediction.bin").read_bytes()
+    rec = 8208
+    count = int.from_bytes(raw[:8], "little")
+    (dcase / "encrypted_prediction.bin").write_bytes((count - 1).to_bytes(8, "little") + raw[8:8 + (count - 1) * rec])
+    assert "no record" in dexpect(dcase, "IDASH_ERR_INDEX")
+
+
+def test_decrypt_truncated_predictions(dcase):
+    raw = (dcase / "encrypted_prediction.bin").read_bytes()
+    (dcase / "encrypted_prediction.bin").write_bytes(raw[:-10])
+    dexpect(dcase, "IDASH_ERR_FORMAT")

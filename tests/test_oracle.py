@@ -93,6 +93,32 @@ def test_decrypted_csv_matches_fixture(oracle, name):
             assert abs(np.float32(ph) - float(vals[v])) <= 1e-5 * max(1.0, abs(float(vals[v])))
 
 
+def oracle_csv(oracle, d, params, preds, by_position=True):
+    """The reference's CSV (write_decrypted_predictions, eval/idash.cpp:436-469)
+    rebuilt from the oracle's decryption: sample-major lines, positions in
+    params order, each float as printf("%.6g") (what an ostream prints)."""
+    key = oracle.read_key(os.path.join(d, "keys.bin"))
+    ns = params["NUM_SAMPLES"]
+    scores = oracle.trlwe_decrypt(np.ascontiguousarray(preds["coef"]), key, ns)
+    row = {int(r["idx"]): i for i, r in enumerate(preds)}
+    out = ["Subject ID,target SNP,0,1,2"]
+    for s in range(ns):
+        for pos, name in params["out_names"]:
+            b = params["out"][pos]
+            vals = ",".join("%.6g" % float(scores[row[b[g]], s]) for g in range(3))
+            out.append(f"{s},{pos if by_position else name},{vals}")
+    return "\n".join(out) + "\n"
+
+
+@pytest.mark.parametrize("name", SMALL_CASES)
+def test_oracle_decrypt_reproduces_reference_csv(oracle, name):
+    """The oracle's decryption (oracle_trlwe_decrypt) formatted as the
+    reference formats it equals the reference decrypt's CSV byte for byte."""
+    d, params, model, data, preds = load_case(oracle, name)
+    assert oracle_csv(oracle, d, params, preds, True) == open(os.path.join(d, "result_bypos.csv")).read()
+    assert oracle_csv(oracle, d, params, preds, False) == open(os.path.join(d, "result.csv")).read()
+
+
 REF_BIN = os.path.join(ROOT, "oracle", "_ref", "cloud")
 
 
