@@ -279,6 +279,37 @@ def section_decrypt(ctx, model, spec, d_out, seed, steps):
                       "4 coefficients per thread over the key's nonzero positions"}
 
 
+def section_encrypt(ctx, spec, seed, steps):
+    """Party A's encryption (encrypt_data_ph1/ph2, eval/idash.cpp:615-679) of
+    the headline's inputs: 16,184 tags x 3 one-hot features = 48,552 fresh
+    TRLWE (1,000 genotypes each, 5% missing), device-resident (CUDA events)."""
+    import numpy as np
+    from idash2019_2_gb300 import gpu
+    rng = np.random.default_rng(seed)
+    n_tags, ns = spec["n_tags"], spec["num_samples"]
+    geno = rng.integers(0, 3, size=(n_tags, ns)).astype(np.int8)
+    geno[rng.random(size=geno.shape) < 0.05] = -1
+    n_rows = 3 * n_tags
+    src = np.arange(n_rows, dtype=np.uint32)  # NUM_REGIONS = 1: row f holds feature f = 3p + v
+    d_geno, d_src = ctx.device_alloc(geno.nbytes), ctx.device_alloc(src.nbytes)
+    d_geno.upload(geno)
+    d_src.upload(src)
+    d_out = ctx.device_alloc(n_rows * gpu.RECORD_BYTES)
+    key = gpu.synth_key(seed)
+    params = gpu.encrypt_params(ns, 1, 1024)
+    run = lambda: gpu.encrypt_device(ctx, params, key, seed, n_rows, d_src.ptr, d_geno.ptr, ns, d_out.ptr,
+                                     gpu.RECORD_OUT)
+    for _ in range(3):
+        run()
+    ms = time_on_stream(ctx, run, steps)
+    for b in (d_geno, d_src, d_out):
+        b.free()
+    return {"value": n_rows / (ms / 1e3), "unit": "TRLWE encryptions/s", "ms_per_step": ms, "rows": n_rows,
+            "samples": ns, "key_weight": int(key.sum()),
+            "kernel": "k_encrypt_rows: one CTA per row, counter-based mask and Box-Muller noise, mask*key over "
+                      "the key's nonzero positions, one-hot messages, record headers"}
+
+
 def section_lwe(ctx, name, seed, n_indiv, n_tags, n_targets, neighbours=5, choices=None, passes=2, chunk=2048):
     """Per-individual LWE form: inputs resident (n_indiv LWE samples of n=1024
     per feature row), outputs produced range by range into a 2-slot HBM ring
@@ -567,11 +598,13 @@ def run_ours(args):
         forms["kinds"] = section_kinds(ctx, w, spec, d_in, d_out, min(args.steps, 200))
     if world == 1 and "decrypt" in sections:
         forms["decrypt"] = section_decrypt(ctx, model, spec, d_out, args.seed + rank, min(args.steps, 50))
+    if world == 1 and "encrypt" in sections:
+        forms["encrypt"] = section_encrypt(ctx, spec, args.seed + rank, min(args.steps, 50))
     d_in.free()
     d_out.free()
     model.free()
     if world == 1:
-        forms.update(run_sections(ctx, args, sections - {"plain", "kinds", "decrypt"}))
+        forms.update(run_sections(ctx, args, sections - {"plain", "kinds", "decrypt", "encrypt"}))
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -603,7 +636,7 @@ def main():
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="trlwe_full")
     ap.add_argument("--seed", type=int, default=0x1DA52019)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--sections", default="plain,kinds,decrypt,lwe_full,batched_uneven,intpoly,serving",
+    ap.add_argument("--sections", default="plain,kinds,encrypt,decrypt,lwe_full,batched_uneven,intpoly,serving",
                     help="extra forms measured after the headline (comma list, '' for none)")
     ap.add_argument("--no-headline", action="store_true",
                     help="measure only --sections (no headline, e2e or CPU baseline)")

@@ -106,6 +106,17 @@ class DecryptReport(C.Structure):
                 ("n_records", C.c_uint64), ("n_lines", C.c_uint64)]
 
 
+class EncryptParams(C.Structure):
+    _fields_ = [("N", C.c_uint32), ("k", C.c_uint32), ("num_samples", C.c_uint32), ("num_regions", C.c_uint32),
+                ("region_size", C.c_uint32), ("one_t32", C.c_int32), ("nan_t32", C.c_int32 * 3),
+                ("record_tag", C.c_int32), ("alpha", C.c_double)]
+
+
+class EncryptReport(C.Structure):
+    _fields_ = [("read_s", C.c_double), ("encrypt_s", C.c_double), ("write_s", C.c_double),
+                ("n_positions", C.c_uint64), ("n_records", C.c_uint64)]
+
+
 # name -> (restype, argtypes); every function include/idash_gpu.h declares.
 PROTOTYPES = {
     "idash_status_string": (C.c_char_p, [status_t]),
@@ -153,6 +164,10 @@ PROTOTYPES = {
                                              vp, C.POINTER(RowLayout), vp, C.POINTER(RowLayout), vp]),
     "idash_cloud_files": (status_t, [C.c_int, C.c_char_p, C.c_char_p, C.c_char_p, C.c_char_p,
                                      C.POINTER(CloudReport), C.c_char_p, C.c_size_t]),
+    "idash_encrypt_trlwe_device": (status_t, [vp, C.POINTER(EncryptParams), i32p, C.c_uint64, C.c_uint64, vp,
+                                              vp, C.c_uint32, vp, vp, vp, C.POINTER(RowLayout), vp, vp]),
+    "idash_encrypt_files": (status_t, [C.c_int, C.c_char_p, C.c_char_p, C.c_char_p, C.c_uint64,
+                                       C.POINTER(EncryptReport), C.c_char_p, C.c_size_t]),
     "idash_decrypt_trlwe_device": (status_t, [vp, i32p, C.c_uint32, vp, C.POINTER(RowLayout), C.c_uint64,
                                               C.c_uint32, vp, vp]),
     "idash_decrypt_files": (status_t, [C.c_int, C.c_char_p, C.c_char_p, C.c_char_p, C.c_int,

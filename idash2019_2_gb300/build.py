@@ -6,6 +6,7 @@ translation unit, in parallel) and links, inside the package directory:
   libidash_gpu.so   the C ABI declared in include/idash_gpu.h
   idash_cloud       the cloud CLI (eval/cloud.cpp's argv and output)
   idash_decrypt     the decryption CLI (eval/decrypt.cpp's argv and output)
+  idash_encrypt     the encryption CLI (eval/encrypt.cpp's argv and output)
 
 Objects go to idash2019_2_gb300/_build/ (git-ignored).
 """
@@ -24,6 +25,7 @@ BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libidash_gpu.so")
 CLI = os.path.join(PKG, "idash_cloud")
 DECRYPT_CLI = os.path.join(PKG, "idash_decrypt")
+ENCRYPT_CLI = os.path.join(PKG, "idash_encrypt")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O3",
@@ -38,10 +40,13 @@ LIB_SOURCES = [
     "csrc/capi.cpp",
     "csrc/plan.cpp",
     "csrc/decrypt.cu",
+    "csrc/encrypt.cu",
     "csrc/host/idash_host.cpp",
     "csrc/host/decrypt_host.cpp",
+    "csrc/host/encrypt_host.cpp",
 ]
-CLIS = {CLI: ["csrc/host/cloud_main.cpp"], DECRYPT_CLI: ["csrc/host/decrypt_main.cpp"]}
+CLIS = {CLI: ["csrc/host/cloud_main.cpp"], DECRYPT_CLI: ["csrc/host/decrypt_main.cpp"],
+        ENCRYPT_CLI: ["csrc/host/encrypt_main.cpp"]}
 
 
 def _nvcc() -> str:

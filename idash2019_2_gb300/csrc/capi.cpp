@@ -316,6 +316,35 @@ bool autotune_wanted(idash_model *m) { return !m->tuned && m->ctx->opt_kernel !=
 
 void idash_set_thread_error(const std::string &msg) { g_open_error = msg; }
 
+namespace idash {
+
+cudaError_t stage_key(const int32_t *key, uint32_t N, cudaStream_t s, StagedKey *out) {
+    *out = StagedKey();
+    std::vector<uint32_t> words;  // positions, then values
+    for (uint32_t i = 0; i < N; ++i)
+        if (key[i] != 0) {
+            words.push_back(i);
+            out->binary = out->binary && key[i] == 1;
+        }
+    out->n_nz = uint32_t(words.size());
+    for (uint32_t q = 0; q < out->n_nz; ++q) words.push_back(uint32_t(key[words[q]]));
+    if (words.empty()) return cudaSuccess;
+    cudaError_t e = cudaMallocAsync(&out->buf, words.size() * 4, s);
+    if (e != cudaSuccess) return e;
+    // pageable source: the copy returns once the bytes are staged
+    e = cudaMemcpyAsync(out->buf, words.data(), words.size() * 4, cudaMemcpyHostToDevice, s);
+    out->idx = static_cast<uint32_t *>(out->buf);
+    out->val = reinterpret_cast<int32_t *>(out->idx + out->n_nz);
+    return e;
+}
+
+void release_key(StagedKey *k, cudaStream_t s) {
+    if (k->buf) cudaFreeAsync(k->buf, s);
+    *k = StagedKey();
+}
+
+}  // namespace idash
+
 cudaEvent_t idash_ctx::event(size_t i) {
     while (events.size() <= i) {
         cudaEvent_t e = nullptr;
@@ -420,7 +449,6 @@ void idash_close(idash_ctx *ctx) {
     cudaFree(ctx->d_counters);
     cudaFree(ctx->d_in_buf);
     cudaFree(ctx->d_out_buf);
-    cudaFree(ctx->d_key_buf);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     if (ctx->h2d) cudaStreamDestroy(ctx->h2d);
     if (ctx->d2h) cudaStreamDestroy(ctx->d2h);

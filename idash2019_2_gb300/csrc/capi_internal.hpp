@@ -27,6 +27,19 @@ cudaError_t fill_uniform_rows(uint64_t seed, uint64_t row_begin, uint64_t n_rows
 cudaError_t digest_words(const uint32_t *words, uint64_t n_words, uint64_t index_base, uint64_t *d_digest,
                          int sm_count, cudaStream_t s);
 uint64_t digest_host(const uint32_t *words, uint64_t n_words, uint64_t index_base);
+
+// The nonzero coefficients of an integer key polynomial (positions, values),
+// staged on the device for launches on `s` and released stream-ordered after
+// them, so concurrent calls with different keys never share a buffer.
+struct StagedKey {
+    uint32_t *idx = nullptr;
+    int32_t *val = nullptr;
+    uint32_t n_nz = 0;
+    bool binary = true;  // every nonzero coefficient is 1
+    void *buf = nullptr;
+};
+cudaError_t stage_key(const int32_t *key, uint32_t N, cudaStream_t s, StagedKey *out);
+void release_key(StagedKey *k, cudaStream_t s);
 }  // namespace idash
 
 // Message returned by idash_last_error(NULL) on this thread (entry points
@@ -59,8 +72,6 @@ struct idash_ctx {
     // buffers for the host-memory path (grow only)
     uint8_t *d_in_buf = nullptr, *d_out_buf = nullptr;
     size_t d_in_cap = 0, d_out_cap = 0;
-    void *d_key_buf = nullptr;  // decryption key's nonzero positions and values (grow only)
-    size_t d_key_cap = 0;
     std::vector<cudaEvent_t> events;
 
     idash_status fail(idash_status s, const std::string &msg) {

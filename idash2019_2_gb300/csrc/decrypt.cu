@@ -10,7 +10,6 @@
 // float(phase / 2^32) equals float(phase) * 2^-32 exactly (scaling by a power
 // of two commutes with round-to-nearest for these magnitudes).
 #include <algorithm>
-#include <vector>
 
 #include "capi_internal.hpp"
 #include "common.cuh"
@@ -19,12 +18,13 @@ namespace idash {
 namespace {
 
 constexpr uint32_t kDecryptThreads = 256;
-constexpr uint32_t kDecryptCols = 4;  // consecutive coefficients per thread
+constexpr uint32_t kDecryptCols = 4;  // coefficients per thread, kDecryptThreads apart
 
 // One CTA per row (grid-stride over rows).  Shared memory: ext[2N], the
 // negacyclic extension of the mask a (ext[N + t] = a[t], ext[t] = -a[t]) so
 // that (a*s)[j] = sum_i s_i * ext[N + j - i]; then the key's nonzero
-// positions (and values, for a non-binary key).
+// positions (and values, for a non-binary key).  Thread t owns coefficients
+// t + 256c: a warp's loads of one key position are consecutive words.
 template <bool kBinary>
 __global__ void __launch_bounds__(kDecryptThreads) k_decrypt_phase(const uint8_t *in, uint64_t in_stride,
                                                                    uint32_t N, uint32_t num_samples,
@@ -47,25 +47,26 @@ __global__ void __launch_bounds__(kDecryptThreads) k_decrypt_phase(const uint8_t
             ext[t] = 0u - v;
         }
         __syncthreads();
-        for (uint32_t j0 = threadIdx.x * kDecryptCols; j0 < num_samples; j0 += blockDim.x * kDecryptCols) {
+        for (uint32_t j0 = threadIdx.x; j0 < num_samples; j0 += kDecryptThreads * kDecryptCols) {
             uint32_t acc[kDecryptCols];
 #pragma unroll
-            for (uint32_t r = 0; r < kDecryptCols; ++r) acc[r] = 0;
-            // j0 is a multiple of 4 below N (a power of two >= 4), so j0 + r < N
-            // and ext[N + j0 + r - i] stays inside [1, 2N) for every i < N
+            for (uint32_t c = 0; c < kDecryptCols; ++c) acc[c] = 0;
+            // coefficient j = j0 + 256c is read only when j < N (N >= 4 may be
+            // smaller than 1024), so ext[N + j - i] stays inside [1, 2N)
             const uint32_t *e = ext + N + j0;
 #pragma unroll 4
             for (uint32_t q = 0; q < n_nz; ++q) {
                 const uint32_t *p = e - idx[q];
                 const uint32_t s = kBinary ? 1u : uint32_t(val[q]);
 #pragma unroll
-                for (uint32_t r = 0; r < kDecryptCols; ++r) acc[r] += kBinary ? p[r] : s * p[r];
+                for (uint32_t c = 0; c < kDecryptCols; ++c)
+                    if (j0 + c * kDecryptThreads < N) acc[c] += kBinary ? p[c * kDecryptThreads] : s * p[c * kDecryptThreads];
             }
 #pragma unroll
-            for (uint32_t r = 0; r < kDecryptCols; ++r) {
-                const uint32_t j = j0 + r;
+            for (uint32_t c = 0; c < kDecryptCols; ++c) {
+                const uint32_t j = j0 + c * kDecryptThreads;
                 if (j < num_samples) {
-                    const uint32_t phase = a[N + j] - acc[r];
+                    const uint32_t phase = a[N + j] - acc[c];
                     out[row * num_samples + j] = __int2float_rn(int32_t(phase)) * 0x1p-32f;
                 }
             }
@@ -82,53 +83,27 @@ extern "C" idash_status idash_decrypt_trlwe_device(idash_ctx *ctx, const int32_t
                                                    const idash_row_layout *in_layout, uint64_t n_rows,
                                                    uint32_t num_samples, float *d_out, void *stream) {
     if (!ctx) return IDASH_ERR_INVALID_ARGUMENT;
-    if (!key || !d_in || !in_layout || !d_out || N < 4 || N > 4096 || (N & (N - 1)) || num_samples == 0 ||
+    if (!key || !d_in || !in_layout || !d_out || N < 4 || N > 2048 || (N & (N - 1)) || num_samples == 0 ||
         num_samples > N)
         return ctx->fail(IDASH_ERR_INVALID_ARGUMENT, "idash_decrypt_trlwe_device: bad arguments");
     if (in_layout->row_stride < uint64_t(2) * N * 4 || in_layout->payload_offset % 4 || in_layout->row_stride % 4)
         return ctx->fail(IDASH_ERR_INVALID_ARGUMENT, "idash_decrypt_trlwe_device: bad row layout");
     if (n_rows == 0) return IDASH_OK;
-    std::vector<uint32_t> idx;
-    std::vector<int32_t> val;
-    bool binary = true;
-    for (uint32_t i = 0; i < N; ++i)
-        if (key[i] != 0) {
-            idx.push_back(i);
-            val.push_back(key[i]);
-            binary = binary && key[i] == 1;
-        }
     cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
-    const size_t key_bytes = std::max<size_t>(idx.size(), 1) * 8;
-    if (ctx->d_key_cap < key_bytes) {
-        cudaFree(ctx->d_key_buf);
-        ctx->d_key_buf = nullptr;
-        ctx->d_key_cap = 0;
-        idash_status st = ctx->check_cuda(cudaMalloc(&ctx->d_key_buf, key_bytes), "cudaMalloc key");
-        if (st != IDASH_OK) return st;
-        ctx->d_key_cap = key_bytes;
-    }
-    uint32_t *d_idx = static_cast<uint32_t *>(ctx->d_key_buf);
-    int32_t *d_val = reinterpret_cast<int32_t *>(d_idx + std::max<size_t>(idx.size(), 1));
-    if (!idx.empty()) {
-        // pageable source: the call returns once the bytes are staged
-        idash_status st = ctx->check_cuda(
-            cudaMemcpyAsync(d_idx, idx.data(), idx.size() * 4, cudaMemcpyHostToDevice, s), "key upload");
-        if (st == IDASH_OK)
-            st = ctx->check_cuda(cudaMemcpyAsync(d_val, val.data(), val.size() * 4, cudaMemcpyHostToDevice, s),
-                                 "key upload");
-        if (st != IDASH_OK) return st;
-    }
-    const uint32_t n_nz = uint32_t(idx.size());
-    const size_t smem = size_t(2) * N * 4 + size_t(n_nz) * (binary ? 4 : 8);
+    StagedKey k;
+    idash_status st = ctx->check_cuda(stage_key(key, N, s, &k), "key upload");
+    if (st != IDASH_OK) return st;
+    const size_t smem = size_t(2) * N * 4 + size_t(k.n_nz) * (k.binary ? 4 : 8);
     const uint32_t blocks = uint32_t(std::min<uint64_t>(n_rows, uint64_t(ctx->sm_count) * 8));
     const uint8_t *in = static_cast<const uint8_t *>(d_in) + in_layout->payload_offset;
-    if (binary)
-        k_decrypt_phase<true><<<blocks, kDecryptThreads, smem, s>>>(in, in_layout->row_stride, N, num_samples, d_idx,
-                                                                   d_val, n_nz, n_rows, d_out);
+    if (k.binary)
+        k_decrypt_phase<true><<<blocks, kDecryptThreads, smem, s>>>(in, in_layout->row_stride, N, num_samples, k.idx,
+                                                                   k.val, k.n_nz, n_rows, d_out);
     else
         k_decrypt_phase<false><<<blocks, kDecryptThreads, smem, s>>>(in, in_layout->row_stride, N, num_samples,
-                                                                    d_idx, d_val, n_nz, n_rows, d_out);
-    idash_status st = ctx->check_cuda(cudaGetLastError(), "k_decrypt_phase launch");
+                                                                    k.idx, k.val, k.n_nz, n_rows, d_out);
+    st = ctx->check_cuda(cudaGetLastError(), "k_decrypt_phase launch");
+    release_key(&k, s);
     if (st == IDASH_OK) ctx->stats.kernel_launches++;
     return st;
 }

@@ -146,6 +146,28 @@ struct IdashKey {
 constexpr int32_t kTlweKeyTag = 52;  // record tag of the key stream format
 Status read_key(IdashKey &key, const std::string &filename);
 
+// ------------------------------------------------------------ encryption
+// eval/idash.h:123-127: per tag position, NUM_SAMPLES genotypes (0/1/2, -1
+// when missing).  Same container as the reference, filled in the same order,
+// so it iterates in the same order.
+struct PlaintextData {
+    std::unordered_map<uint64_t, std::vector<int8_t>> data;
+};
+// read_plaintext_data (eval/idash.cpp:280-309).
+Status read_plaintext_data(PlaintextData &plain, const IdashParams &params, const std::string &filename);
+// Every plaintext position is an input position of params, and the features
+// fill the reference's ciphertext pool (eval/idash.cpp:621-641).
+Status check_plaintext(const PlaintextData &plain, const IdashParams &params);
+// dtot32 (a double on the torus -> Torus32, fractional part truncated).
+int32_t dtot32(double d);
+// encrypt_data_ph1 + ph2 (eval/idash.cpp:615-679) on the GPU: one record
+// per FeatIndex, in the order the reference's EncryptedData map iterates.
+// seed: the mask / noise generator's key.
+Status encrypt_data(EncryptedData &enc, const PlaintextData &plain, const IdashKey &key, idash_ctx *ctx,
+                    uint64_t seed);
+// write_encrypted_data (eval/idash.cpp:536-556): one bulk write.
+Status write_encrypted_data(const EncryptedData &enc, const std::string &filename);
+
 // eval/idash.h:190-211, held as one matrix: the scores of the prediction
 // file's record r at [r * num_samples, (r + 1) * num_samples).
 struct DecryptedPredictions {

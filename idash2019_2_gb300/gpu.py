@@ -459,3 +459,44 @@ def synth_key(seed: int, N: int = 1024) -> np.ndarray:
     out = np.zeros(N, np.int32)
     _lib.load().idash_synth_key(seed, N, _p(out, C.c_int32))
     return out
+
+
+def encrypt_params(num_samples: int, num_regions: int, region_size: int, alpha: float = 2.0 ** -25,
+                   N: int = 1024) -> "_lib.EncryptParams":
+    """Encryption parameters with the reference's message encodings
+    (ONE_IN_T32 and the NaN one-hot values, eval/idash.cpp:29-45)."""
+    def dtot32(d):
+        return int(((d - int(d)) * 4294967296.0)) & 0xFFFFFFFF
+
+    p = _lib.EncryptParams()
+    p.N, p.k, p.num_samples, p.num_regions, p.region_size = N, 1, num_samples, num_regions, region_size
+    p.one_t32 = dtot32(1.0 / 16384)
+    for v, frac in enumerate((3.0 / 6.0, 2.0 / 6.0, 1.0 / 6.0)):
+        p.nan_t32[v] = dtot32(frac / 16384)
+    p.record_tag = 42
+    p.alpha = alpha
+    return p
+
+
+def encrypt_device(ctx: Context, params, key: np.ndarray, seed: int, n_rows: int, d_slot_src: int, d_geno: int,
+                   geno_stride: int, d_out: int, layout: RowLayout, d_row_index: int = 0, d_row_out: int = 0,
+                   d_noise: int = 0, stream=None):
+    """Fresh TRLWE encryptions with one-hot messages (idash_encrypt_trlwe_device)."""
+    key = np.ascontiguousarray(key, np.int32)
+    vp = lambda x: C.c_void_p(x) if x else None
+    ctx.check(ctx.lib.idash_encrypt_trlwe_device(ctx.h, C.byref(params), _p(key, C.c_int32), seed, n_rows,
+                                                 vp(d_slot_src), vp(d_geno), geno_stride, vp(d_row_index),
+                                                 vp(d_row_out), C.c_void_p(d_out), C.byref(layout), vp(d_noise),
+                                                 vp(stream)))
+
+
+def encrypt_files(keys_file: str, challenge_file: str, data_file: str, seed: int, device: int = 0) -> dict:
+    """eval/encrypt.cpp's flow on files (idash_encrypt_files)."""
+    lib = _lib.load()
+    rep = _lib.EncryptReport()
+    err = C.create_string_buffer(1024)
+    code = lib.idash_encrypt_files(device, keys_file.encode(), challenge_file.encode(), data_file.encode(), seed,
+                                   C.byref(rep), err, len(err))
+    if code != 0:
+        raise IdashError(code, err.value.decode(errors="replace"))
+    return {k: getattr(rep, k) for k, _ in rep._fields_}

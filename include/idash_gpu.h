@@ -314,6 +314,57 @@ typedef struct {
 idash_status idash_cloud_files(int device, const char *params_file, const char *model_dir, const char *data_file,
                                const char *pred_file, idash_cloud_report *report, char *errbuf, size_t errbuf_len);
 
+/* ------------------------------------------- encryption (party A)
+ * encrypt_data_ph1 + encrypt_data_ph2 (eval/idash.cpp:615-679) on the
+ * device.  Row r (of n_rows) becomes a fresh TRLWE encryption of zero under
+ * `key` (tLweSymEncryptZero, :625): mask a uniform, noise e Gaussian with
+ * standard deviation alpha on the torus (truncated as dtot32), b = a*s + e;
+ * then the one-hot messages are added as setScore does (eval/idash.h:152-156):
+ * for region g < num_regions and sample s < num_samples, coefficient
+ * b[g*region_size + s] gains the value of plaintext feature
+ * src = d_slot_src[r*num_regions + g] (3p + v: genotype row p, genotype
+ * value v; 0xFFFFFFFF: none): one_t32 when d_geno[p*geno_stride + s] == v,
+ * nan_t32[v] when that genotype is not 0, 1 or 2 (missing), else 0.
+ * Row r is written at output row d_row_out[r] (NULL: r); with a header in
+ * out_layout it gets index d_row_index[r] (NULL: r) and record_tag, and the
+ * variance field gets alpha^2.  Masks and noise come from a counter-based
+ * generator keyed by `seed` (a statistical generator, as TFHE's is, not a
+ * cryptographic one).  d_noise (optional, n_rows * N int32) receives e.
+ * key: N integer coefficients in host memory; N a power of two in [4, 2048].
+ * Asynchronous on `stream` once the key has been staged. */
+typedef struct {
+    uint32_t N, k;          /* k must be 1 */
+    uint32_t num_samples;   /* NUM_SAMPLES */
+    uint32_t num_regions;   /* NUM_REGIONS */
+    uint32_t region_size;   /* REGION_SIZE */
+    int32_t one_t32;        /* ONE_IN_T32 = dtot32(2^-14) (eval/idash.cpp:39) */
+    int32_t nan_t32[3];     /* NAN_{0,1,2}_IN_T32 = dtot32({3,2,1}/6 * 2^-14) (:40-45) */
+    int32_t record_tag;     /* tag written into record headers */
+    double alpha;           /* noise standard deviation on the torus (IdashParams::alpha = 2^-25) */
+} idash_encrypt_params;
+idash_status idash_encrypt_trlwe_device(idash_ctx *ctx, const idash_encrypt_params *params, const int32_t *key,
+                                        uint64_t seed, uint64_t n_rows, const uint32_t *d_slot_src,
+                                        const int8_t *d_geno, uint32_t geno_stride, const uint32_t *d_row_index,
+                                        const uint32_t *d_row_out, void *d_out, const idash_row_layout *out_layout,
+                                        int32_t *d_noise, void *stream);
+
+/* eval/encrypt.cpp:14-38 as one call: reads keys.bin and the challenge file
+ * of tag genotypes (read_plaintext_data, eval/idash.cpp:280-309: lines
+ * "22 <pos> <pos> <name> <g_0> ... <g_{NUM_SAMPLES-1}>", a genotype other than
+ * 0/1/2 counts as missing), encrypts on `device`, and writes
+ * encrypted_data.bin with the records (FeatIndex, tag, TRLWE, variance) in the
+ * order the reference writes them (:536-556).  The ciphertexts differ from
+ * the reference's (another random generator); they decrypt to the same
+ * messages.  seed 0 draws a fresh seed from the operating system. */
+typedef struct {
+    double read_s;     /* key + challenge file reads */
+    double encrypt_s;  /* planning, kernel, device->host copy */
+    double write_s;    /* encrypted_data.bin write */
+    uint64_t n_positions, n_records;
+} idash_encrypt_report;
+idash_status idash_encrypt_files(int device, const char *keys_file, const char *challenge_file, const char *data_file,
+                                 uint64_t seed, idash_encrypt_report *report, char *errbuf, size_t errbuf_len);
+
 /* ------------------------------------------- decryption (party A)
  * decrypt_predictions (eval/idash.cpp:682-761) on the device: for each of
  * n_rows TRLWE rows (k = 1, layout in_layout), the phase b - a*s (tLwePhase,
@@ -321,7 +372,7 @@ idash_status idash_cloud_files(int device, const char *params_file, const char *
  * at coefficients [0, num_samples), converted as t32tod to float:
  * d_out[r * num_samples + j] = float(phase_r[j] / 2^32).  key: the key's N
  * integer coefficients in host memory (binary for TFHE keys; any integers
- * are accepted).  N a power of two in [4, 4096].  Asynchronous on `stream`
+ * are accepted).  N a power of two in [4, 2048].  Asynchronous on `stream`
  * once the key has been staged (the call synchronises with `stream` first). */
 idash_status idash_decrypt_trlwe_device(idash_ctx *ctx, const int32_t *key, uint32_t N, const void *d_in,
                                         const idash_row_layout *in_layout, uint64_t n_rows, uint32_t num_samples,

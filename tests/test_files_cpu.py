@@ -132,3 +132,54 @@ def test_decrypt_truncated_predictions(dcase):
     raw = (dcase / "encrypted_prediction.bin").read_bytes()
     (dcase / "encrypted_prediction.bin").write_bytes(raw[:-10])
     dexpect(dcase, "IDASH_ERR_FORMAT")
+
+
+# ------------------------------------------------ encryption inputs (party A)
+@pytest.fixture()
+def ecase(tmp_path):
+    try:
+        gpu._lib.load()
+    except ImportError as e:
+        pytest.skip(str(e))
+    src = os.path.join(GOLDEN, "ref_r10")
+    for f in ["keys.bin", "tags.txt"]:
+        shutil.copy(os.path.join(src, f), tmp_path / f)
+    return tmp_path
+
+
+def eexpect(d, name, keys="keys.bin", tags="tags.txt"):
+    with pytest.raises(gpu.IdashError) as e:
+        gpu.encrypt_files(str(d / keys), str(d / tags), str(d / "enc.bin"), seed=1, device=0)
+    assert e.value.name == name, str(e.value)
+    assert not (d / "enc.bin").exists()
+    return str(e.value)
+
+
+def test_encrypt_missing_challenge(ecase):
+    assert "nope.txt" in eexpect(ecase, "IDASH_ERR_IO", tags="nope.txt")
+
+
+def test_encrypt_missing_key(ecase):
+    eexpect(ecase, "IDASH_ERR_IO", keys="nope.bin")
+
+
+def test_encrypt_bad_chromosome_field(ecase):
+    lines = (ecase / "tags.txt").read_text().splitlines()
+    lines[3] = "21" + lines[3][2:]
+    (ecase / "tags.txt").write_text("\n".join(lines) + "\n")
+    assert "22" in eexpect(ecase, "IDASH_ERR_FORMAT")
+
+
+def test_encrypt_missing_positions(ecase):
+    lines = (ecase / "tags.txt").read_text().splitlines()
+    (ecase / "tags.txt").write_text("\n".join(lines[:-2]) + "\n")
+    assert "missing positions" in eexpect(ecase, "IDASH_ERR_FORMAT")
+
+
+def test_encrypt_unknown_position(ecase):
+    lines = (ecase / "tags.txt").read_text().splitlines()
+    f = lines[0].split()
+    f[1] = f[2] = "999999999"
+    lines[0] = " ".join(f)
+    (ecase / "tags.txt").write_text("\n".join(lines) + "\n")
+    assert "not an input position" in eexpect(ecase, "IDASH_ERR_FORMAT")
