@@ -45,6 +45,10 @@ WORKLOADS = {
 }
 METRIC = "encrypted predictions/s (indiv x target x 3)"
 UNIT = "predictions/s"
+# The reference's one published run of this step: 1,004 individuals x 80,882
+# targets x 3 in 3.06433 s of "fhe wall time" on a 4-thread laptop
+# (README.md:220-245), i.e. about 79.5 M predictions/s.
+PUBLISHED_PREDICTIONS_PER_S = 1004 * 80882 * 3 / 3.06433
 KERNEL_NAMES = {0: "window (batched, persistent, CUDA graph)", 1: "direct (plain)",
                 2: "pipe (batched, double-buffered, persistent, CUDA graph)",
                 3: "ws (batched, warp-specialised producer + consumers over an mbarrier ring, CUDA graph)"}
@@ -189,7 +193,8 @@ def run_reference(args):
     el = time.perf_counter() - t0
     value = preds * steps / el
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": steps, "warmup": args.warmup,
-            "ms_per_step": el / steps * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "ms_per_step": el / steps * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": value / PUBLISHED_PREDICTIONS_PER_S if args.workload == "trlwe_full" else None,
             "dtype": "int32 (Z/2^32)", "data": "synthetic (seeded)", "impl": "reference",
             "config": {"workload": spec["desc"]},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
@@ -276,7 +281,7 @@ def section_decrypt(ctx, model, spec, d_out, seed, steps):
             "rows": model.n_out, "samples": ns, "key_weight": nz,
             "word_adds_per_s": adds / (ms / 1e3),
             "kernel": "k_decrypt_phase: one CTA per row, negacyclic extension of the mask in shared memory, "
-                      "4 coefficients per thread over the key's nonzero positions"}
+                      "4 coefficients per thread (256 apart) over the key's nonzero positions"}
 
 
 def section_encrypt(ctx, spec, seed, steps):
@@ -609,7 +614,8 @@ def run_ours(args):
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
-                "vs_baseline": None, "dtype": "int32 (Z/2^32)", "data": "synthetic (seeded)",
+                "vs_baseline": value / PUBLISHED_PREDICTIONS_PER_S if args.workload == "trlwe_full" else None,
+                "dtype": "int32 (Z/2^32)", "data": "synthetic (seeded)",
                 "config": {"workload": spec["desc"], "individuals": spec["n_indiv"], "targets": spec["n_targets"],
                            "tags": spec["n_tags"], "neighbours": spec["neighbours"], "outputs": model.n_out,
                            "input_rows": spec["n_rows"], "l2": "inputs 0.40 GB and outputs 1.99 GB exceed the 129 MB L2",
