@@ -102,6 +102,9 @@ idash_status build_and_upload(idash_model *m, const Candidate &c) {
     lim.max_slots = c.slots;
     lim.max_terms = c.terms;
     lim.max_groups = c.groups;
+    // batched kinds split neighbourhoods larger than one window into parts
+    // (later launches accumulate); the direct kernel reads global memory
+    lim.split = c.kind != KernelKind::kDirect && ctx->opt_split != 0;
     Plan plan;
     bool index_error = false;
     const std::string err = build_plan(in, lim, &plan, &index_error);
@@ -188,13 +191,37 @@ idash_status launch(idash_model *m, const ScoreArgs &a, cudaStream_t s) {
     return st;
 }
 
-// Block range [lo, hi) whose outputs intersect [o_begin, o_end).
-void block_range(const idash_model *m, uint64_t o_begin, uint64_t o_end, uint32_t *lo, uint32_t *hi) {
+uint32_t n_phases(const idash_model *m) {
+    return m->plan.phase_begin.size() > 1 ? uint32_t(m->plan.phase_begin.size() - 1) : 1u;
+}
+
+// Blocks [lo, hi) of phase p whose outputs intersect [o_begin, o_end).
+void block_range(const idash_model *m, uint32_t p, uint64_t o_begin, uint64_t o_end, uint32_t *lo, uint32_t *hi) {
     const auto &B = m->plan.blocks;
-    const auto first = std::partition_point(B.begin(), B.end(), [&](const PlanBlock &b) { return b.out_hi <= o_begin; });
-    const auto last = std::partition_point(first, B.end(), [&](const PlanBlock &b) { return b.out_lo < o_end; });
+    const auto &P = m->plan.phase_begin;
+    const auto b0 = B.begin() + (P.size() > 1 ? P[p] : 0);
+    const auto b1 = B.begin() + (P.size() > 1 ? P[p + 1] : B.size());
+    const auto first = std::partition_point(b0, b1, [&](const PlanBlock &b) { return b.out_hi <= o_begin; });
+    const auto last = std::partition_point(first, b1, [&](const PlanBlock &b) { return b.out_lo < o_end; });
     *lo = uint32_t(first - B.begin());
     *hi = uint32_t(last - B.begin());
+}
+
+// Launches the scoring kernel over every phase's blocks that touch outputs
+// [o_lo, o_hi), phase by phase on `s` (later phases add to what earlier ones
+// wrote); args(b_lo, b_hi) builds one launch's arguments.
+template <class F>
+idash_status launch_phases(idash_model *m, uint64_t o_lo, uint64_t o_hi, cudaStream_t s, F args) {
+    for (uint32_t p = 0; p < n_phases(m); ++p) {
+        uint32_t lo, hi;
+        block_range(m, p, o_lo, o_hi, &lo, &hi);
+        if (lo == hi) continue;
+        ScoreArgs a = args(lo, hi);
+        a.accumulate = p > 0 ? 1u : 0u;
+        idash_status st = launch(m, a, s);
+        if (st != IDASH_OK) return st;
+    }
+    return IDASH_OK;
 }
 
 // Enqueues the whole device-path TRLWE scoring (kernel + record finalize).
@@ -202,9 +229,10 @@ idash_status enqueue_trlwe(idash_model *m, const void *d_in, const idash_row_lay
                            const idash_row_layout *ol, cudaStream_t s) {
     const uint8_t *in = static_cast<const uint8_t *>(d_in);
     uint8_t *out = static_cast<uint8_t *>(d_out);
-    ScoreArgs a = make_args(m, in + il->payload_offset, il->row_stride, out + ol->payload_offset, ol->row_stride,
-                            row_words_of(m, 0), 0, uint32_t(m->plan.blocks.size()), 0, m->n_out, 0);
-    idash_status st = launch(m, a, s);
+    idash_status st = launch_phases(m, 0, m->n_out, s, [&](uint32_t lo, uint32_t hi) {
+        return make_args(m, in + il->payload_offset, il->row_stride, out + ol->payload_offset, ol->row_stride,
+                         row_words_of(m, 0), lo, hi, 0, m->n_out, 0);
+    });
     if (st != IDASH_OK) return st;
     FinalizeArgs f{};
     f.var_ptr = m->d_var_ptr;
@@ -245,13 +273,12 @@ float time_candidate(idash_model *m, const void *d_in, const idash_row_layout *i
 float time_candidate_lwe(idash_model *m, uint32_t n_indiv, const int32_t *d_in, uint64_t in_stride, uint64_t o_lo,
                          uint64_t o_hi, int32_t *d_out, uint64_t out_stride, cudaStream_t s, int reps) {
     cudaEvent_t e0 = m->ctx->event(0), e1 = m->ctx->event(1);
-    uint32_t b_lo, b_hi;
-    block_range(m, o_lo, o_hi, &b_lo, &b_hi);
     const uint32_t rw = row_words_of(m, n_indiv);
     auto run = [&]() {
-        ScoreArgs a = make_args(m, reinterpret_cast<const uint8_t *>(d_in), in_stride * 4,
-                                reinterpret_cast<uint8_t *>(d_out), out_stride * 4, rw, b_lo, b_hi, o_lo, o_hi, o_lo);
-        return launch(m, a, s);
+        return launch_phases(m, o_lo, o_hi, s, [&](uint32_t lo, uint32_t hi) {
+            return make_args(m, reinterpret_cast<const uint8_t *>(d_in), in_stride * 4,
+                             reinterpret_cast<uint8_t *>(d_out), out_stride * 4, rw, lo, hi, o_lo, o_hi, o_lo);
+        });
     };
     if (run() != IDASH_OK) return -1.f;
     cudaEventRecord(e0, s);
@@ -495,6 +522,8 @@ idash_status idash_set_option(idash_ctx *ctx, const char *name, int64_t value) {
     } else if (n == "max_group_terms") {
         if (value < 0) return ctx->fail(IDASH_ERR_INVALID_ARGUMENT, "max_group_terms must be >= 0");
         ctx->opt_max_group_terms = value;
+    } else if (n == "split") {
+        ctx->opt_split = value ? 1 : 0;
     } else {
         return ctx->fail(IDASH_ERR_INVALID_ARGUMENT, "unknown option " + n);
     }
@@ -510,6 +539,7 @@ idash_status idash_get_option(const idash_ctx *ctx, const char *name, int64_t *v
     else if (n == "graph") *value = ctx->opt_graph;
     else if (n == "max_window_slots") *value = ctx->opt_max_window_slots;
     else if (n == "max_group_terms") *value = ctx->opt_max_group_terms;
+    else if (n == "split") *value = ctx->opt_split;
     else return IDASH_ERR_INVALID_ARGUMENT;
     return IDASH_OK;
 }
@@ -779,9 +809,10 @@ idash_status idash_score_trlwe_host(idash_model *m, const void *h_in, const idas
         if ((s = ctx->check_cuda(cudaStreamSynchronize(ctx->stream), "sync")) != IDASH_OK) return s;
     }
 
-    // Chunks of whole blocks; each chunk waits only for the input rows it
-    // reads, and its outputs stream back while later chunks compute.
-    const uint32_t nb = uint32_t(m->plan.blocks.size());
+    // Chunks of whole phase-0 blocks (which cover every output once); each
+    // chunk waits only for the input rows it reads, its later-phase parts
+    // run after it, and its outputs stream back while later chunks compute.
+    const uint32_t nb = m->plan.phase_begin.size() > 1 ? m->plan.phase_begin[1] : uint32_t(m->plan.blocks.size());
     const uint32_t n_chunks = std::max<uint32_t>(1, std::min<uint32_t>(nb, 12));
     std::vector<uint32_t> cb(n_chunks + 1);
     for (uint32_t c = 0; c <= n_chunks; ++c) cb[c] = uint32_t(uint64_t(nb) * c / n_chunks);
@@ -792,6 +823,12 @@ idash_status idash_score_trlwe_host(idash_model *m, const void *h_in, const idas
     for (uint32_t c = 0; c < n_chunks; ++c) {
         uint32_t need = 0;
         for (uint32_t b = cb[c]; b < cb[c + 1]; ++b) need = std::max(need, m->plan.block_max_row[b] + 1);
+        if (cb[c + 1] > cb[c])
+            for (uint32_t p = 1; p < n_phases(m); ++p) {
+                uint32_t lo, hi;
+                block_range(m, p, m->plan.blocks[cb[c]].out_lo, m->plan.blocks[cb[c + 1] - 1].out_hi, &lo, &hi);
+                for (uint32_t b = lo; b < hi; ++b) need = std::max(need, m->plan.block_max_row[b] + 1);
+            }
         if (need > rows_sent) {
             // send the rows in [rows_sent, need) plus a lookahead of the next chunk's share
             uint64_t upto = std::min<uint64_t>(n_in_rows, std::max<uint64_t>(need, rows_sent + (n_in_rows + n_chunks - 1) / n_chunks));
@@ -808,10 +845,13 @@ idash_status idash_score_trlwe_host(idash_model *m, const void *h_in, const idas
         }
         if (cb[c + 1] == cb[c]) continue;
         const uint64_t o_lo = m->plan.blocks[cb[c]].out_lo, o_hi = m->plan.blocks[cb[c + 1] - 1].out_hi;
-        ScoreArgs a = make_args(m, d_in + il->payload_offset, il->row_stride, d_out + ol->payload_offset,
-                                ol->row_stride, row_words, cb[c], cb[c + 1], o_lo, o_hi, 0);
-        a.out_row_map = nullptr;
-        if ((s = launch(m, a, ctx->stream)) != IDASH_OK) return s;
+        s = launch_phases(m, o_lo, o_hi, ctx->stream, [&](uint32_t lo, uint32_t hi) {
+            ScoreArgs a = make_args(m, d_in + il->payload_offset, il->row_stride, d_out + ol->payload_offset,
+                                    ol->row_stride, row_words, lo, hi, o_lo, o_hi, 0);
+            a.out_row_map = nullptr;
+            return a;
+        });
+        if (s != IDASH_OK) return s;
         FinalizeArgs f{};
         f.var_ptr = m->d_var_ptr;
         f.var_row = m->d_var_row;
@@ -847,13 +887,15 @@ idash_status idash_score_trlwe_host(idash_model *m, const void *h_in, const idas
 idash_status idash_model_input_rows(const idash_model *m, uint64_t out_begin, uint64_t out_end, uint64_t *row_begin,
                                     uint64_t *row_end) {
     if (!m || !row_begin || !row_end || out_begin > out_end || out_end > m->n_out) return IDASH_ERR_INVALID_ARGUMENT;
-    uint32_t b_lo, b_hi;
-    block_range(m, out_begin, out_end, &b_lo, &b_hi);
     uint64_t lo = UINT64_MAX, hi = 0;
-    for (uint32_t b = b_lo; b < b_hi; ++b) {
-        if (m->plan.blocks[b].n_slots == 0) continue;
-        lo = std::min<uint64_t>(lo, m->plan.block_min_row[b]);
-        hi = std::max<uint64_t>(hi, uint64_t(m->plan.block_max_row[b]) + 1);
+    for (uint32_t p = 0; p < n_phases(m); ++p) {
+        uint32_t b_lo, b_hi;
+        block_range(m, p, out_begin, out_end, &b_lo, &b_hi);
+        for (uint32_t b = b_lo; b < b_hi; ++b) {
+            if (m->plan.blocks[b].n_slots == 0) continue;
+            lo = std::min<uint64_t>(lo, m->plan.block_min_row[b]);
+            hi = std::max<uint64_t>(hi, uint64_t(m->plan.block_max_row[b]) + 1);
+        }
     }
     if (lo == UINT64_MAX) lo = hi = 0;
     *row_begin = lo;
@@ -882,17 +924,18 @@ idash_status idash_score_trlwe_range(idash_model *m, uint64_t out_begin, uint64_
     if (r_hi > r_lo && (r_lo < in_row_base || r_hi > in_row_base + n_in_rows))
         return ctx->fail(IDASH_ERR_INDEX, "the outputs read input rows outside [in_row_base, in_row_base + n_in_rows)");
     cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
-    uint32_t b_lo, b_hi;
-    block_range(m, out_begin, out_end, &b_lo, &b_hi);
     const uint8_t *in = static_cast<const uint8_t *>(d_in);
     uint8_t *out = static_cast<uint8_t *>(d_out);
-    ScoreArgs a = make_args(m, in + il->payload_offset, il->row_stride, out + ol->payload_offset, ol->row_stride,
-                            row_words_of(m, 0), b_lo, b_hi, out_begin, out_end, out_begin);
-    a.out_row_map = nullptr;
-    a.row_base = uint32_t(in_row_base);
-    a.n_rows = uint32_t(n_in_rows);
-    if (num_samples) a.num_samples = num_samples;
-    if ((s = launch(m, a, st)) != IDASH_OK) return s;
+    s = launch_phases(m, out_begin, out_end, st, [&](uint32_t lo, uint32_t hi) {
+        ScoreArgs a = make_args(m, in + il->payload_offset, il->row_stride, out + ol->payload_offset, ol->row_stride,
+                                row_words_of(m, 0), lo, hi, out_begin, out_end, out_begin);
+        a.out_row_map = nullptr;
+        a.row_base = uint32_t(in_row_base);
+        a.n_rows = uint32_t(n_in_rows);
+        if (num_samples) a.num_samples = num_samples;
+        return a;
+    });
+    if (s != IDASH_OK) return s;
     FinalizeArgs f{};
     f.var_ptr = m->d_var_ptr;
     f.var_row = m->d_var_row;
@@ -938,14 +981,14 @@ idash_status idash_score_lwe_device(idash_model *m, uint32_t n_indiv, const int3
         if ((s = ctx->check_cuda(cudaStreamWaitEvent(cs, ctx->join_in, 0), "join")) != IDASH_OK) return s;
     }
     if (autotune_wanted(m)) {
-        // tune on (at most) the first ~64 blocks of this range
+        // tune on (at most) the first ~64 phase-0 blocks of this range
         uint32_t b_lo, b_hi;
-        block_range(m, out_begin, out_end, &b_lo, &b_hi);
         float best = -1.f;
         Candidate best_c{};
         for (const Candidate &c : candidates(m)) {
             if (build_and_upload(m, c) != IDASH_OK) continue;
-            block_range(m, out_begin, out_end, &b_lo, &b_hi);
+            block_range(m, 0, out_begin, out_end, &b_lo, &b_hi);
+            if (b_hi == b_lo) continue;
             const uint32_t hi = std::min<uint32_t>(b_hi, b_lo + 64);
             const uint64_t o_hi = std::min<uint64_t>(out_end, m->plan.blocks[hi - 1].out_hi);
             const float ms = time_candidate_lwe(m, n_indiv, d_in, in_row_stride, out_begin, o_hi, d_out,
@@ -964,18 +1007,21 @@ idash_status idash_score_lwe_device(idash_model *m, uint32_t n_indiv, const int3
         }
         m->tuned = true;
     }
-    uint32_t b_lo, b_hi;
-    block_range(m, out_begin, out_end, &b_lo, &b_hi);
     const uint32_t rw = row_words_of(m, n_indiv);
     const uint32_t n_slices = (rw + m->slice_words - 1) / m->slice_words;
-    // split so each launch stays below 2^31 tiles
+    // split so each launch stays below 2^31 tiles; phases in order
     const uint32_t per_launch = std::max<uint32_t>(1, uint32_t((1ull << 30) / n_slices));
-    for (uint32_t lo = b_lo; lo < b_hi; lo += per_launch) {
-        const uint32_t hi = std::min(b_hi, lo + per_launch);
-        ScoreArgs a = make_args(m, reinterpret_cast<const uint8_t *>(d_in), in_row_stride * 4,
-                                reinterpret_cast<uint8_t *>(d_out), out_row_stride * 4, rw, lo, hi, out_begin, out_end,
-                                out_begin);
-        if ((s = launch(m, a, cs)) != IDASH_OK) return s;
+    for (uint32_t p = 0; p < n_phases(m); ++p) {
+        uint32_t b_lo, b_hi;
+        block_range(m, p, out_begin, out_end, &b_lo, &b_hi);
+        for (uint32_t lo = b_lo; lo < b_hi; lo += per_launch) {
+            const uint32_t hi = std::min(b_hi, lo + per_launch);
+            ScoreArgs a = make_args(m, reinterpret_cast<const uint8_t *>(d_in), in_row_stride * 4,
+                                    reinterpret_cast<uint8_t *>(d_out), out_row_stride * 4, rw, lo, hi, out_begin,
+                                    out_end, out_begin);
+            a.accumulate = p > 0 ? 1u : 0u;
+            if ((s = launch(m, a, cs)) != IDASH_OK) return s;
+        }
     }
     if (user && user != cs) {
         if ((s = ctx->check_cuda(cudaEventRecord(ctx->join_out, cs), "join")) != IDASH_OK) return s;

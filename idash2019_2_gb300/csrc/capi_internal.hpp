@@ -64,6 +64,7 @@ struct idash_ctx {
     int64_t opt_graph = 1;
     int64_t opt_max_window_slots = 0;
     int64_t opt_max_group_terms = 0;
+    int64_t opt_split = 1;  // batched plans split neighbourhoods larger than a window
 
     idash_stats stats{};
     std::string last_error;

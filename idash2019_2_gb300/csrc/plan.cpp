@@ -110,12 +110,16 @@ std::string build_plan(const PlanInput &in, const PlanLimits &lim, Plan *plan, b
 
     // 2. Groups of up to group_size consecutive outputs with (nearly) the
     //    same slot set: union no larger than 5/4 of the largest member + 1.
+    //    With lim.split, a group larger than one window becomes parts.
     struct G {
         uint64_t o0;
         uint32_t n;
+        uint32_t phase = 0;  // part index of a split group
         std::vector<uint64_t> keys;
         std::vector<uint32_t> c[3];
     };
+    const size_t cap = std::min<size_t>(lim.max_slots, lim.max_terms);
+    if (cap == 0) return "a block must hold at least one slot and one term";
     std::vector<G> groups;
     groups.reserve(n_out / lim.group_size + 1);
     for (uint64_t o = 0; o < n_out;) {
@@ -127,7 +131,8 @@ std::string build_plan(const PlanInput &in, const PlanLimits &lim, Plan *plan, b
             const size_t np = nptr[p + 1] - nptr[p];
             const size_t u = union_size(keys.data(), keys.size(), nkey.data() + nptr[p], np);
             const size_t big = std::max(largest, np);
-            if (u > big + big / 4 + 1 || u > lim.max_slots || u > lim.max_terms) break;
+            if (u > big + big / 4 + 1) break;
+            if (!lim.split && (u > lim.max_slots || u > lim.max_terms)) break;
             std::vector<uint64_t> merged;
             merged.reserve(u);
             std::set_union(keys.begin(), keys.end(), nkey.begin() + nptr[p], nkey.begin() + nptr[p + 1],
@@ -149,81 +154,107 @@ std::string build_plan(const PlanInput &in, const PlanLimits &lim, Plan *plan, b
                 g.c[m][idx] = ncoef[t];
             }
         }
-        if (keys.size() > lim.max_slots || keys.size() > lim.max_terms)
+        if (g.keys.size() <= cap) {
+            groups.push_back(std::move(g));
+        } else if (!lim.split) {
             return "an output needs more window slots than one block holds";
-        groups.push_back(std::move(g));
+        } else {
+            // parts of at most `cap` consecutive slots; part k runs in phase k
+            for (size_t k0 = 0, part = 0; k0 < g.keys.size(); k0 += cap, ++part) {
+                const size_t k1 = std::min(g.keys.size(), k0 + cap);
+                G gp;
+                gp.o0 = g.o0;
+                gp.n = g.n;
+                gp.phase = uint32_t(part);
+                gp.keys.assign(g.keys.begin() + k0, g.keys.begin() + k1);
+                for (uint32_t m = 0; m < 3; ++m) gp.c[m].assign(g.c[m].begin() + k0, g.c[m].begin() + k1);
+                groups.push_back(std::move(gp));
+            }
+        }
         o += n;
     }
+    uint32_t n_phases = 1;
+    for (const G &g : groups) n_phases = std::max(n_phases, g.phase + 1);
+    // per phase, its groups in output order
+    std::vector<std::vector<uint32_t>> by_phase(n_phases);
+    for (uint32_t q = 0; q < groups.size(); ++q) by_phase[groups[q].phase].push_back(q);
 
-    // 3. Blocks of consecutive groups sharing one window of slots.
+    // 3. Blocks of consecutive groups (of one phase) sharing one window of slots.
     std::vector<uint64_t> win;
-    size_t gi = 0;
-    while (gi < groups.size()) {
-        PlanBlock b{};
-        b.group_begin = uint32_t(plan->groups.size());
-        b.term_begin = uint32_t(plan->terms.size());
-        b.slot_begin = uint32_t(plan->slots.size());
-        win.clear();
-        size_t gend = gi;
-        uint32_t terms = 0;
-        while (gend < groups.size()) {
-            const G &g = groups[gend];
-            const size_t u = union_size(win.data(), win.size(), g.keys.data(), g.keys.size());
-            if (gend > gi && (u > lim.max_slots || terms + g.keys.size() > lim.max_terms ||
-                              gend - gi + 1 > lim.max_groups))
-                break;
-            std::vector<uint64_t> merged;
-            merged.reserve(u);
-            std::set_union(win.begin(), win.end(), g.keys.begin(), g.keys.end(), std::back_inserter(merged));
-            win.swap(merged);
-            terms += uint32_t(g.keys.size());
-            ++gend;
-        }
-        if (win.size() > 0xFFFFu) return "a block window needs more than 65535 slots";
-        // unrotated slots first (bulk-copied by the kernel), rotated ones after
-        // (gathered with the negacyclic sign); both parts stay sorted
-        const size_t n_unrot = size_t(std::count_if(win.begin(), win.end(),
-                                                    [](uint64_t k) { return (k & 0xFFFFFFFFu) == 0; }));
-        std::stable_partition(win.begin(), win.end(), [](uint64_t k) { return (k & 0xFFFFFFFFu) == 0; });
-        auto local_of = [&](uint64_t key) -> uint32_t {
-            const auto lo = (key & 0xFFFFFFFFu) == 0 ? win.begin() : win.begin() + n_unrot;
-            const auto hi = (key & 0xFFFFFFFFu) == 0 ? win.begin() + n_unrot : win.end();
-            return uint32_t(std::lower_bound(lo, hi, key) - win.begin());
-        };
-        b.n_slots = uint16_t(win.size());
-        b.n_rot = uint16_t(win.size() - n_unrot);
-        uint32_t max_row = 0, min_row = win.empty() ? 0u : 0xFFFFFFFFu;
-        for (uint64_t k : win) {
-            plan->slots.push_back(PlanSlot{uint32_t(k >> 32), uint32_t(k & 0xFFFFFFFFu)});
-            max_row = std::max(max_row, uint32_t(k >> 32));
-            min_row = std::min(min_row, uint32_t(k >> 32));
-        }
-        plan->block_max_row.push_back(max_row);
-        plan->block_min_row.push_back(min_row);
-        b.out_lo = uint32_t(groups[gi].o0);
-        b.out_hi = uint32_t(groups[gend - 1].o0 + groups[gend - 1].n);
-        for (size_t q = gi; q < gend; ++q) {
-            const G &g = groups[q];
-            PlanGroup pg{};
-            pg.term_begin = uint32_t(plan->terms.size()) - b.term_begin;
-            pg.n_terms = uint32_t(g.keys.size());
-            for (uint32_t m = 0; m < 3; ++m) {
-                pg.out[m] = m < g.n ? uint32_t(g.o0 + m) : kNoOutput;
-                pg.bias[m] = m < g.n ? int32_t(bias[g.o0 + m]) : 0;
+    for (uint32_t ph = 0; ph < n_phases; ++ph) {
+        plan->phase_begin.push_back(uint32_t(plan->blocks.size()));
+        const std::vector<uint32_t> &order = by_phase[ph];
+        size_t gi = 0;
+        while (gi < order.size()) {
+            PlanBlock b{};
+            b.group_begin = uint32_t(plan->groups.size());
+            b.term_begin = uint32_t(plan->terms.size());
+            b.slot_begin = uint32_t(plan->slots.size());
+            win.clear();
+            size_t gend = gi;
+            uint32_t terms = 0;
+            while (gend < order.size()) {
+                const G &g = groups[order[gend]];
+                const size_t u = union_size(win.data(), win.size(), g.keys.data(), g.keys.size());
+                if (gend > gi && (u > lim.max_slots || terms + g.keys.size() > lim.max_terms ||
+                                  gend - gi + 1 > lim.max_groups))
+                    break;
+                std::vector<uint64_t> merged;
+                merged.reserve(u);
+                std::set_union(win.begin(), win.end(), g.keys.begin(), g.keys.end(), std::back_inserter(merged));
+                win.swap(merged);
+                terms += uint32_t(g.keys.size());
+                ++gend;
             }
-            for (size_t t = 0; t < g.keys.size(); ++t)
-                plan->terms.push_back(
-                    PlanTerm{int32_t(g.c[0][t]), int32_t(g.c[1][t]), int32_t(g.c[2][t]), local_of(g.keys[t])});
-            plan->groups.push_back(pg);
+            if (win.size() > 0xFFFFu) return "a block window needs more than 65535 slots";
+            // unrotated slots first (bulk-copied by the kernel), rotated ones
+            // after (gathered with the negacyclic sign); both parts stay sorted
+            const size_t n_unrot = size_t(std::count_if(win.begin(), win.end(),
+                                                        [](uint64_t k) { return (k & 0xFFFFFFFFu) == 0; }));
+            std::stable_partition(win.begin(), win.end(), [](uint64_t k) { return (k & 0xFFFFFFFFu) == 0; });
+            auto local_of = [&](uint64_t key) -> uint32_t {
+                const auto lo = (key & 0xFFFFFFFFu) == 0 ? win.begin() : win.begin() + n_unrot;
+                const auto hi = (key & 0xFFFFFFFFu) == 0 ? win.begin() + n_unrot : win.end();
+                return uint32_t(std::lower_bound(lo, hi, key) - win.begin());
+            };
+            b.n_slots = uint16_t(win.size());
+            b.n_rot = uint16_t(win.size() - n_unrot);
+            uint32_t max_row = 0, min_row = win.empty() ? 0u : 0xFFFFFFFFu;
+            for (uint64_t k : win) {
+                plan->slots.push_back(PlanSlot{uint32_t(k >> 32), uint32_t(k & 0xFFFFFFFFu)});
+                max_row = std::max(max_row, uint32_t(k >> 32));
+                min_row = std::min(min_row, uint32_t(k >> 32));
+            }
+            plan->block_max_row.push_back(max_row);
+            plan->block_min_row.push_back(min_row);
+            const G &first = groups[order[gi]], &last = groups[order[gend - 1]];
+            b.out_lo = uint32_t(first.o0);
+            b.out_hi = uint32_t(last.o0 + last.n);
+            for (size_t q = gi; q < gend; ++q) {
+                const G &g = groups[order[q]];
+                PlanGroup pg{};
+                pg.term_begin = uint32_t(plan->terms.size()) - b.term_begin;
+                pg.n_terms = uint32_t(g.keys.size());
+                for (uint32_t m = 0; m < 3; ++m) {
+                    pg.out[m] = m < g.n ? uint32_t(g.o0 + m) : kNoOutput;
+                    // the bias goes with the first part only
+                    pg.bias[m] = m < g.n && g.phase == 0 ? int32_t(bias[g.o0 + m]) : 0;
+                }
+                for (size_t t = 0; t < g.keys.size(); ++t)
+                    plan->terms.push_back(PlanTerm{int32_t(g.c[0][t]), int32_t(g.c[1][t]), int32_t(g.c[2][t]),
+                                                   local_of(g.keys[t])});
+                plan->groups.push_back(pg);
+            }
+            b.n_groups = uint32_t(gend - gi);
+            b.n_terms = uint32_t(plan->terms.size()) - b.term_begin;
+            plan->max_block_slots = std::max<uint32_t>(plan->max_block_slots, b.n_slots);
+            plan->max_block_terms = std::max(plan->max_block_terms, b.n_terms);
+            plan->max_block_groups = std::max(plan->max_block_groups, b.n_groups);
+            plan->blocks.push_back(b);
+            gi = gend;
         }
-        b.n_groups = uint32_t(gend - gi);
-        b.n_terms = uint32_t(plan->terms.size()) - b.term_begin;
-        plan->max_block_slots = std::max<uint32_t>(plan->max_block_slots, b.n_slots);
-        plan->max_block_terms = std::max(plan->max_block_terms, b.n_terms);
-        plan->max_block_groups = std::max(plan->max_block_groups, b.n_groups);
-        plan->blocks.push_back(b);
-        gi = gend;
     }
+    plan->phase_begin.push_back(uint32_t(plan->blocks.size()));
     return "";
 }
 

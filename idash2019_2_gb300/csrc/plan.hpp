@@ -74,10 +74,18 @@ struct PlanLimits {
     uint32_t max_slots = 48;    // window slots per block
     uint32_t max_terms = 2048;  // terms per block
     uint32_t max_groups = 64;   // groups per block
+    // A group whose slots exceed one window is split into parts of at most
+    // min(max_slots, max_terms) slots; part p is planned in phase p, whose
+    // launch adds its partial sums to the outputs phase p - 1 wrote.
+    bool split = false;
 };
 
 struct Plan {
     std::vector<PlanBlock> blocks;
+    // Blocks of phase p are [phase_begin[p], phase_begin[p + 1]), each phase
+    // in output order.  Phase 0 writes every output (with its bias); a later
+    // phase holds the further parts of split groups and accumulates.
+    std::vector<uint32_t> phase_begin;
     std::vector<PlanSlot> slots;
     std::vector<PlanGroup> groups;
     std::vector<PlanTerm> terms;

@@ -110,6 +110,26 @@ __device__ __forceinline__ void write_outputs(const ScoreArgs &a, const PlanGrou
         }
         const uint64_t r = a.out_row_map ? uint64_t(a.out_row_map[o]) : uint64_t(o) - a.out_row_base;
         uint8_t *row = a.out + r * a.out_stride + uint64_t(c0) * 4;
+        if (a.accumulate) {
+            // a later part of a split group: add what the earlier launches
+            // wrote (zeroed columns stay zero: both terms are zero there)
+#pragma unroll
+            for (int k = 0; k < Q; ++k) {
+                const uint32_t q = 4 * lane + 4 * k * TEAM;
+                if (q + 4 <= valid) {
+                    const int4 v = ldg_nc_v4(row + size_t(q) * 4);
+                    acc[m][4 * k + 0] += uint32_t(v.x);
+                    acc[m][4 * k + 1] += uint32_t(v.y);
+                    acc[m][4 * k + 2] += uint32_t(v.z);
+                    acc[m][4 * k + 3] += uint32_t(v.w);
+                } else {
+                    const uint32_t *p = reinterpret_cast<const uint32_t *>(row) + q;
+#pragma unroll
+                    for (int e = 0; e < 4; ++e)
+                        if (q + e < valid) acc[m][4 * k + e] += p[e];
+                }
+            }
+        }
         if (valid >= W) {  // a full slice: every quad is inside the row
 #pragma unroll
             for (int k = 0; k < Q; ++k)

@@ -34,6 +34,7 @@ struct ScoreArgs {
     uint32_t lwe_n1;                       // LWE: n + 1 words per sample
     uint32_t max_slots, max_terms, max_groups;  // shared-memory carve-up (one buffer)
     uint32_t n_stages;                          // warp-specialised kernel: buffers in the ring
+    uint32_t accumulate;          // 1: add to the outputs (later parts of split groups)
     uint32_t *tile_counter;       // persistent kernel: next tile (zeroed before launch)
     uint32_t *err;                // device error word
 };

@@ -74,7 +74,10 @@ idash_status idash_sync(idash_ctx *ctx);
  * persistent only, 4 warp-specialised producer/consumer ring only),
  * "slice_words" (0 = autotune; 128..2048), "ctas_per_sm",
  * "graph" (0/1: replay launches from a CUDA graph), "max_window_slots",
- * "max_group_terms". */
+ * "max_group_terms", "split" (1, the default: the batched kernels take
+ * neighbourhoods larger than one shared-memory window in parts, later parts
+ * adding to the outputs in follow-up launches; 0: such models fall back to
+ * the plain kernel). */
 idash_status idash_set_option(idash_ctx *ctx, const char *name, int64_t value);
 idash_status idash_get_option(const idash_ctx *ctx, const char *name, int64_t *value);
 

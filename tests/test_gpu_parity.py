@@ -177,11 +177,13 @@ def test_trlwe_regions_persistent_kernels(ctx, oracle, kernel):
 
 
 def test_large_neighbourhoods_fall_back_to_direct_kernel(ctx, oracle):
-    """50-neighbour outputs (150 window slots) do not fit a 2048-word slice
-    window; the model is planned for the direct kernel and stays exact."""
+    """With splitting off, 50-neighbour outputs (150 window slots) do not fit
+    a 2048-word slice window; the model is planned for the direct kernel and
+    stays exact."""
     w = gpu.synth_model(seed=31, n_tags=200, n_targets=300, choices=[5, 50])
     rows = random_rows(9, 600)
     ctx.set_option("slice_words", 2048)
+    ctx.set_option("split", 0)
     try:
         m = gpu.TrlweModel(ctx, w.model, 600, 1000, 1, 1024)
         assert m.info()["kernel"] == 1
@@ -189,8 +191,58 @@ def test_large_neighbourhoods_fall_back_to_direct_kernel(ctx, oracle):
         m.free()
     finally:
         ctx.set_option("slice_words", 0)
+        ctx.set_option("split", 1)
     want, _ = oracle.trlwe_score(w.model.term_ptr, w.model.term_feat, w.model.term_coef, rows, 1000, 1, 1024)
     np.testing.assert_array_equal(got, want)
+
+
+@pytest.mark.parametrize("kernel,slice_words,regions", [(2, 2048, 1), (4, 2048, 1), (4, 512, 3), (3, 1024, 10),
+                                                        (2, 256, 1)])
+def test_split_neighbourhoods_device_and_host(ctx, oracle, kernel, slice_words, regions):
+    """Neighbourhoods of up to 150 slots with windows of a few slots: the
+    plan splits them into parts whose later launches add to the outputs
+    (record layout with variance, device path with and without graph, host
+    path and output ranges), bit-exact to the oracle."""
+    rs = 1024 // regions
+    ns = min(rs, 1000) - (1 if regions > 1 else 0)
+    w = gpu.synth_model(seed=37 + regions, n_tags=120, n_targets=200, choices=[5, 50, 1, 20])
+    n_rows = (3 * 120 + regions - 1) // regions
+    rows = random_rows(11 + regions, n_rows)
+    ctx.set_option("kernel", kernel)
+    ctx.set_option("slice_words", slice_words)
+    ctx.set_option("max_window_slots", 24)
+    try:
+        m = gpu.TrlweModel(ctx, w.model, n_rows, ns, regions, rs)
+        want, _ = oracle.trlwe_score(w.model.term_ptr, w.model.term_feat, w.model.term_coef, rows, ns, regions, rs)
+        for graph in (1, 0):
+            ctx.set_option("graph", graph)
+            np.testing.assert_array_equal(m.score(rows), want)
+        info = m.info()
+        assert info["kernel"] == KIND_OF_OPTION[kernel] and info["max_window_slots"] <= 24
+        # host path (chunked, phases per chunk)
+        lay = gpu.DENSE_TRLWE
+        h_in, h_out = ctx.host_alloc(rows.nbytes), ctx.host_alloc(m.n_out * 8192)
+        h_in.array[:] = rows.view(np.uint8).reshape(-1)
+        m.score_host(h_in.ptr, lay, n_rows, h_out.ptr, lay)
+        np.testing.assert_array_equal(np.frombuffer(h_out.array, np.int32).reshape(m.n_out, 2048), want)
+        # output ranges
+        d_in = ctx.device_alloc(rows.nbytes)
+        d_in.upload(rows)
+        for lo, hi in [(0, m.n_out), (7, 100), (301, 302)]:
+            d_out = ctx.device_alloc((hi - lo) * 8192)
+            m.score_range(lo, hi, 0, d_in.ptr, lay, 0, n_rows, d_out.ptr, lay)
+            ctx.sync()
+            np.testing.assert_array_equal(d_out.download(dtype=np.int32).reshape(hi - lo, 2048), want[lo:hi])
+            d_out.free()
+        d_in.free()
+        h_in.free()
+        h_out.free()
+        m.free()
+    finally:
+        ctx.set_option("kernel", 0)
+        ctx.set_option("slice_words", 0)
+        ctx.set_option("max_window_slots", 0)
+        ctx.set_option("graph", 1)
 
 
 def test_trlwe_autotune_picks_a_correct_plan(ctx, oracle):
@@ -207,11 +259,12 @@ def test_trlwe_autotune_picks_a_correct_plan(ctx, oracle):
     assert info["kernel"] in (0, 2, 3) and info["slice_words"] in (512, 1024, 2048)
 
 
-@pytest.mark.parametrize("kernel,slice_words", [(0, 0), (2, 128), (3, 256), (3, 512), (1, 256), (4, 256),
-                                                (4, 512), (4, 1024)])
-def test_lwe_vs_oracle_ranges(ctx, oracle, kernel, slice_words):
+@pytest.mark.parametrize("kernel,slice_words,split", [(0, 0, 1), (2, 128, 1), (3, 256, 1), (3, 512, 1), (1, 256, 1),
+                                                      (4, 256, 1), (4, 512, 1), (4, 1024, 1), (4, 1024, 0)])
+def test_lwe_vs_oracle_ranges(ctx, oracle, kernel, slice_words, split):
     # (4, 1024): a 10-neighbour output needs 30 slots of 4 KiB, more than one
-    # ring stage holds, so the plan falls back to the direct kernel.
+    # ring stage holds: the plan splits it into parts, or, with splitting
+    # off, falls back to the direct kernel.
     n, n_indiv, n_tags = 1024, 37, 60
     w = gpu.synth_model(seed=9, n_tags=n_tags, n_targets=90, choices=[5, 10, 2])
     n_feat = 3 * n_tags
@@ -222,6 +275,7 @@ def test_lwe_vs_oracle_ranges(ctx, oracle, kernel, slice_words):
     rows = d_in.download(dtype=np.int32).reshape(n_feat, stride)
     ctx.set_option("kernel", kernel)
     ctx.set_option("slice_words", slice_words)
+    ctx.set_option("split", split)
     try:
         m = gpu.LweModel(ctx, w.model, n_feat, n_indiv, n)
         for (lo, hi, ni) in [(0, m.n_out, n_indiv), (5, 131, n_indiv), (100, 101, n_indiv), (0, m.n_out, 11)]:
@@ -234,7 +288,7 @@ def test_lwe_vs_oracle_ranges(ctx, oracle, kernel, slice_words):
             want = oracle.lwe_score(w.model.term_ptr, w.model.term_feat, w.model.term_coef, sub, ni, lo, hi, n=n)
             np.testing.assert_array_equal(got, want)
             d_out.free()
-        if (kernel, slice_words) == (4, 1024):
+        if (kernel, slice_words, split) == (4, 1024, 0):
             assert m.info()["kernel"] == 1
         elif slice_words:
             assert m.info()["slice_words"] == slice_words
@@ -242,6 +296,7 @@ def test_lwe_vs_oracle_ranges(ctx, oracle, kernel, slice_words):
     finally:
         ctx.set_option("kernel", 0)
         ctx.set_option("slice_words", 0)
+        ctx.set_option("split", 1)
     d_in.free()
 
 
