@@ -363,14 +363,16 @@ def section_lwe(ctx, name, seed, n_indiv, n_tags, n_targets, neighbours=5, choic
     return out
 
 
-def section_intpoly(ctx, seed, passes=5):
+def section_intpoly(ctx, seed, passes=5, scale=1):
     """Integer-polynomial x TRLWE product at full scale: 48,552 input TRLWE
     (16,184 tags x 3), 242,646 outputs (80,882 targets x 3), 20 neighbours
     (60 dense int16 weight polynomials per output, |w| <= 8192), one block of
-    1,024 individuals per TRLWE.  Exact (two-prime NTT + CRT)."""
+    1,024 individuals per TRLWE.  Exact (two-prime NTT + CRT).  scale > 1
+    divides the tag and target counts (profiling size)."""
     import numpy as np
     from idash2019_2_gb300 import gpu
-    w = gpu.synth_model(seed, 16184, 80882, neighbours=20)
+    n_tags, n_targets = 16184 // scale, 80882 // scale
+    w = gpu.synth_model(seed, n_tags, n_targets, neighbours=20)
     csr = w.model
     const = csr.term_feat == 0xFFFFFFFF
     counts = np.diff(csr.term_ptr.astype(np.int64)) - np.add.reduceat(const.astype(np.int64),
@@ -381,7 +383,7 @@ def section_intpoly(ctx, seed, passes=5):
     owner = np.repeat(np.arange(csr.n_out), np.diff(csr.term_ptr.astype(np.int64)))
     bias[owner[const]] = csr.term_coef[const]
     icsr = gpu.CSRModel(ptr, feat, np.zeros(len(feat), np.int32))
-    n_terms, n_rows = len(feat), 3 * 16184
+    n_terms, n_rows = len(feat), 3 * n_tags
     d_poly = ctx.device_alloc(n_terms * 1024 * 2)
     gpu.synth_int16_device(ctx, seed, n_terms * 1024, 8192, d_poly.ptr)
     t0 = time.perf_counter()
@@ -390,7 +392,7 @@ def section_intpoly(ctx, seed, passes=5):
     d_poly.free()
     params = gpu.TrlweParams(1024, 1, 1024, 1, 1024, 1 << 18, 42)
     d_in = ctx.device_alloc(n_rows * 8192)
-    gpu.synth_trlwe_device(ctx, seed, params, 16184, d_in.ptr, gpu.DENSE_TRLWE)
+    gpu.synth_trlwe_device(ctx, seed, params, n_tags, d_in.ptr, gpu.DENSE_TRLWE)
     d_out = ctx.device_alloc(csr.n_out * 8192)
     run = lambda: m.score_device(d_in.ptr, gpu.DENSE_TRLWE, 0, csr.n_out, d_out.ptr, gpu.DENSE_TRLWE)
     run()
@@ -406,8 +408,9 @@ def section_intpoly(ctx, seed, passes=5):
            "resident_weight_bytes": n_terms * 2 * 1024 * 4,
            "roofline": {"bound": "hbm", "achieved": traffic / (ms / 1e3) / 1e9, "peak": peak, "unit": "GB/s",
                         "frac": traffic / (ms / 1e3) / 1e9 / peak, "algorithmic_bytes_per_step": traffic},
-           "workload": "integer-polynomial x TRLWE: 48,552 input TRLWE, 242,646 outputs, 60 dense int16 weight "
-                       "polynomials per output, N=1024, 1,024 individuals per TRLWE (predictions = outputs x 1024)"}
+           "workload": f"integer-polynomial x TRLWE: {n_rows:,} input TRLWE, {csr.n_out:,} outputs, 60 dense int16 "
+                       "weight polynomials per output, N=1024, 1,024 individuals per TRLWE (predictions = outputs x "
+                       "1024)"}
     for b in (d_in, d_out):
         b.free()
     m.free()
@@ -478,7 +481,7 @@ def run_sections(ctx, args, sections):
                                                    "neighbours uniform from {5,10,20,30,50}", args.seed + 1,
                                               ni, nt, ng, choices=[5, 10, 20, 30, 50], passes=1)
     if "intpoly" in sections:
-        forms["intpoly"] = section_intpoly(ctx, args.seed + 3)
+        forms["intpoly"] = section_intpoly(ctx, args.seed + 3, scale=64 if args.small else 1)
     if "serving" in sections:
         forms["serving"] = section_serving(ctx, args.seed + 2)
     return forms
