@@ -50,6 +50,7 @@ struct Candidate {
     KernelKind kind;
     uint32_t w, g, slots, terms, groups, cps;
     uint32_t stages = 1;  // kWs: buffers in the ring
+    bool split = false;   // plan neighbourhoods larger than a window as parts
 };
 
 // Shared-memory carve-up of one buffer: a window-kernel CTA for `cps` CTAs
@@ -104,7 +105,7 @@ idash_status build_and_upload(idash_model *m, const Candidate &c) {
     lim.max_groups = c.groups;
     // batched kinds split neighbourhoods larger than one window into parts
     // (later launches accumulate); the direct kernel reads global memory
-    lim.split = c.kind != KernelKind::kDirect && ctx->opt_split != 0;
+    lim.split = c.split && c.kind != KernelKind::kDirect;
     Plan plan;
     bool index_error = false;
     const std::string err = build_plan(in, lim, &plan, &index_error);
@@ -318,6 +319,16 @@ std::vector<Candidate> candidates(idash_model *m) {
         if (use_ws)  // one 512-thread CTA per SM (register file)
             for (uint32_t stages : {2u, 3u})
                 if (window_limits(ctx, KernelKind::kWs, w, 1, &c, stages)) out.push_back(c);
+    }
+    // then the same shapes with split plans: used only when no shape fits
+    // the model whole (the autotuner skips them once one has)
+    if (ctx->opt_split) {
+        const size_t n = out.size();
+        for (size_t i = 0; i < n; ++i) {
+            Candidate c = out[i];
+            c.split = true;
+            out.push_back(c);
+        }
     }
     return out;
 }
@@ -716,6 +727,7 @@ idash_status idash_score_trlwe_device(idash_model *m, const void *d_in, const id
         float best = -1.f;
         Candidate best_c{};
         for (const Candidate &c : candidates(m)) {
+            if (c.split && best >= 0) break;
             if (build_and_upload(m, c) != IDASH_OK) continue;
             const float ms = time_candidate(m, d_in, il, d_out, ol, cs, 3);
             if (ms > 0 && (best < 0 || ms < best)) {
@@ -986,6 +998,7 @@ idash_status idash_score_lwe_device(idash_model *m, uint32_t n_indiv, const int3
         float best = -1.f;
         Candidate best_c{};
         for (const Candidate &c : candidates(m)) {
+            if (c.split && best >= 0) break;
             if (build_and_upload(m, c) != IDASH_OK) continue;
             block_range(m, 0, out_begin, out_end, &b_lo, &b_hi);
             if (b_hi == b_lo) continue;
