@@ -186,96 +186,125 @@ struct IntpolyArgs {
     uint32_t *err;
 };
 
-constexpr int kScoreThreads = 512;   // k_intpoly_score: 2 polynomials x 256 quads
-constexpr uint32_t kRowStage = 256;   // term rows staged in shared memory per pass
+constexpr int kScoreThreads = 256;   // k_intpoly_score: thread x owns NTT points 4x..4x+3
+constexpr uint32_t kScoreStages = 3;  // terms in flight per CTA
 
-// Montgomery reduction without the final correction: a value in [0, 2p)
-// congruent to a*b*2^-32 mod p (a, b < p < 2^31).
-__device__ __forceinline__ uint32_t mont_mul_lazy(uint32_t a, uint32_t b, uint32_t p, uint32_t pinv) {
-    const uint64_t t = uint64_t(a) * b;
-    const uint32_t m = uint32_t(t) * pinv;
-    return uint32_t((t + uint64_t(m) * p) >> 32);
+__device__ __forceinline__ void ip_mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
 }
 
-// One CTA per output (grid-stride).  Thread x: polynomial x / 256 (mask a or
-// body b) and NTT points 4q..4q+3, q = x % 256, of both primes.  The output's
-// term rows are staged in shared memory first; each term's weights and input
-// transforms are loaded one term ahead of the arithmetic; products are summed
-// unreduced in 64 bits (each < 2p, so any realistic term count fits) and
-// reduced once.  Then inverse NTT, CRT and the a1 epilogue.
+// Stage layout: one term's weight transform (2 primes x N words) then the
+// input row's transform (2 polynomials x 2 primes x N words).
+__host__ __device__ constexpr uint32_t ip_stage_words(uint32_t N) { return 6 * N; }
+
+// One CTA per output (grid-stride), a bulk-copy pipeline over the terms.
+// Thread 0 keeps kScoreStages terms in flight: each term's weight transform
+// (8 KiB) and input-row transform (16 KiB) are copied with cp.async.bulk into
+// a ring stage and completed on that stage's mbarrier; the CTA computes on the
+// oldest stage (thread x: NTT points 4x..4x+3 of the four arrays), agrees at a
+// barrier that the stage is free, and thread 0 refills it with the term
+// kScoreStages ahead, across output boundaries.  Then inverse NTT, CRT and
+// the a1 epilogue.  Every wait is bounded; a CTA whose copy never lands
+// drains its copies in flight and stops.
 __global__ void __launch_bounds__(kScoreThreads) k_intpoly_score(const IntpolyArgs a) {
-    extern __shared__ uint32_t sh[];
-    uint32_t *itws = sh;                 // 2 * N inverse twiddles
-    uint32_t *arr = sh + 2 * a.N;        // 4 arrays: [poly * 2 + prime][N]
-    uint32_t *rows_s = arr + 4 * a.N;    // kRowStage staged term rows
+    extern __shared__ __align__(128) uint8_t ip_smem[];
     const uint32_t N = a.N;
-    for (uint32_t x = threadIdx.x; x < 2 * N; x += blockDim.x) itws[x] = a.itw[x];
-    const uint32_t quad = threadIdx.x & 255u, poly = threadIdx.x >> 8;
-    const uint32_t p0 = a.k.p[0], p1 = a.k.p[1], i0 = a.k.pinv[0], i1 = a.k.pinv[1];
-    for (uint64_t o = a.out_begin + blockIdx.x; o < a.out_end; o += gridDim.x) {
-        uint64_t acc[2][4];  // [prime][point]
-#pragma unroll
-        for (int q = 0; q < 2; ++q)
-#pragma unroll
-            for (int e = 0; e < 4; ++e) acc[q][e] = 0;
-        const uint64_t t_begin = a.term_ptr[o], t_end = a.term_ptr[o + 1];
-        for (uint64_t c0 = t_begin; c0 < t_end; c0 += kRowStage) {
-            const uint32_t nt = t_end - c0 < kRowStage ? uint32_t(t_end - c0) : kRowStage;
-            __syncthreads();  // the previous pass is done with rows_s
-            for (uint32_t i = threadIdx.x; i < nt; i += blockDim.x) {
-                uint32_t r = a.term_row[c0 + i];
-                if (r >= a.n_rows) {
-                    report_error(a.err, kDevBadIndex);
-                    r = 0xFFFFFFFFu;
-                }
-                rows_s[i] = r;
-            }
-            __syncthreads();
-            uint4 w0, w1, x0, x1;  // this term: weights (prime 0, 1), input transform (prime 0, 1)
-            auto fetch = [&](uint32_t i, uint4 &fw0, uint4 &fw1, uint4 &fx0, uint4 &fx1) {
-                const uint32_t r = rows_s[i];
-                if (r == 0xFFFFFFFFu) {
-                    fw0 = fw1 = fx0 = fx1 = make_uint4(0, 0, 0, 0);
-                    return;
-                }
-                const uint4 *wv = reinterpret_cast<const uint4 *>(a.w_hat + (c0 + i) * 2 * N);
-                const uint4 *cv = reinterpret_cast<const uint4 *>(a.c_hat + uint64_t(r) * 4 * N);
-                fw0 = wv[quad];
-                fw1 = wv[N / 4 + quad];
-                fx0 = cv[(2 * poly) * (N / 4) + quad];
-                fx1 = cv[(2 * poly + 1) * (N / 4) + quad];
-            };
-            fetch(0, w0, w1, x0, x1);
-            for (uint32_t i = 0; i < nt; ++i) {
-                uint4 nw0, nw1, nx0, nx1;
-                if (i + 1 < nt) fetch(i + 1, nw0, nw1, nx0, nx1);
-                acc[0][0] += mont_mul_lazy(w0.x, x0.x, p0, i0);
-                acc[0][1] += mont_mul_lazy(w0.y, x0.y, p0, i0);
-                acc[0][2] += mont_mul_lazy(w0.z, x0.z, p0, i0);
-                acc[0][3] += mont_mul_lazy(w0.w, x0.w, p0, i0);
-                acc[1][0] += mont_mul_lazy(w1.x, x1.x, p1, i1);
-                acc[1][1] += mont_mul_lazy(w1.y, x1.y, p1, i1);
-                acc[1][2] += mont_mul_lazy(w1.z, x1.z, p1, i1);
-                acc[1][3] += mont_mul_lazy(w1.w, x1.w, p1, i1);
-                if (i + 1 < nt) {
-                    w0 = nw0;
-                    w1 = nw1;
-                    x0 = nx0;
-                    x1 = nx1;
-                }
+    uint64_t *full = reinterpret_cast<uint64_t *>(ip_smem);                     // [kScoreStages]
+    uint32_t *stage0 = reinterpret_cast<uint32_t *>(ip_smem + 128);             // kScoreStages x 6N
+    uint32_t *arr = stage0 + kScoreStages * ip_stage_words(N);                  // 4 arrays of N
+    uint32_t *itws = arr + 4 * N;                                               // 2N inverse twiddles
+    const uint32_t tid = threadIdx.x;
+    if (tid == 0) {
+        for (uint32_t s = 0; s < kScoreStages; ++s) mbar_init(&full[s], 1);
+        fence_mbar_init();
+    }
+    for (uint32_t x = tid; x < 2 * N; x += blockDim.x) itws[x] = a.itw[x];
+    __syncthreads();
+
+    // Fetch cursor (thread 0): the next (output, term) of this CTA's
+    // sequence, with that term's input row loaded one issue ahead so its
+    // latency hides behind a term's arithmetic.
+    uint64_t f_o = a.out_begin + blockIdx.x, f_t = 0, f_end = 0;
+    uint32_t pre_r = 0;
+    uint64_t issued = 0;  // terms issued so far (stage = index % kScoreStages)
+    auto advance = [&]() {
+        while (f_o < a.out_end && f_t >= f_end) {  // skip finished and empty outputs
+            f_o += gridDim.x;
+            if (f_o < a.out_end) {
+                f_t = a.term_ptr[f_o];
+                f_end = a.term_ptr[f_o + 1];
             }
         }
-        __syncthreads();  // the previous output's readers of arr are done
+        if (f_o < a.out_end) pre_r = a.term_row[f_t];
+    };
+    auto issue_next = [&]() {
+        if (f_o >= a.out_end) return;
+        uint32_t r = pre_r;
+        if (r >= a.n_rows) {
+            report_error(a.err, kDevBadIndex);
+            r = 0;  // read a valid row; the output is reported invalid
+        }
+        const uint32_t s = uint32_t(issued % kScoreStages);
+        uint32_t *st = stage0 + s * ip_stage_words(N);
+        fence_proxy_async_smem();
+        ip_mbar_expect_tx(&full[s], 6 * N * 4);
+        bulk_g2s(st, a.w_hat + f_t * 2 * N, 2 * N * 4, &full[s]);
+        bulk_g2s(st + 2 * N, a.c_hat + uint64_t(r) * 4 * N, 4 * N * 4, &full[s]);
+        ++issued;
+        ++f_t;
+        advance();
+    };
+    if (tid == 0 && f_o < a.out_end) {
+        f_t = a.term_ptr[f_o];
+        f_end = a.term_ptr[f_o + 1];
+        advance();
+    }
+    if (tid == 0)
+        for (uint32_t i = 0; i < kScoreStages; ++i) issue_next();
+
+    const uint32_t p0 = a.k.p[0], p1 = a.k.p[1], i0 = a.k.pinv[0], i1 = a.k.pinv[1];
+    uint64_t consumed = 0;
+    bool ok = true;
+    for (uint64_t o = a.out_begin + blockIdx.x; o < a.out_end && ok; o += gridDim.x) {
+        uint32_t acc[16];  // [poly * 2 + prime][4]
 #pragma unroll
-        for (int q = 0; q < 2; ++q)
+        for (int e = 0; e < 16; ++e) acc[e] = 0;
+        const uint64_t nt = a.term_ptr[o + 1] - a.term_ptr[o];
+        for (uint64_t i = 0; i < nt; ++i) {
+            const uint32_t s = uint32_t(consumed % kScoreStages);
+            const bool got = mbar_wait_bounded(&full[s], uint32_t((consumed / kScoreStages) & 1u), a.err);
+            const uint32_t *st = stage0 + s * ip_stage_words(N);
+            const uint4 *wv = reinterpret_cast<const uint4 *>(st);
+            const uint4 *cv = reinterpret_cast<const uint4 *>(st + 2 * N);
+            const uint4 w0 = wv[tid], w1 = wv[N / 4 + tid];
+            const uint32_t W[2][4] = {{w0.x, w0.y, w0.z, w0.w}, {w1.x, w1.y, w1.z, w1.w}};
 #pragma unroll
-            for (int e = 0; e < 4; ++e) arr[(2 * poly + q) * N + 4 * quad + e] = uint32_t(acc[q][e] % a.k.p[q]);
+            for (int ap = 0; ap < 4; ++ap) {  // (poly, prime)
+                const uint4 c = cv[ap * (N / 4) + tid];
+                const uint32_t Cv[4] = {c.x, c.y, c.z, c.w};
+                const int q = ap & 1;
+                const uint32_t p = q ? p1 : p0, pinv = q ? i1 : i0;
+#pragma unroll
+                for (int e = 0; e < 4; ++e) acc[ap * 4 + e] = mod_add(acc[ap * 4 + e], mont_mul(W[q][e], Cv[e], p, pinv), p);
+            }
+            ++consumed;
+            // every thread is done with stage s (and agrees the copy landed)
+            ok = __syncthreads_and(got ? 1 : 0) != 0;
+            if (!ok) break;
+            if (tid == 0) issue_next();
+        }
+        if (!ok) break;
+#pragma unroll
+        for (int ap = 0; ap < 4; ++ap)
+#pragma unroll
+            for (int e = 0; e < 4; ++e) arr[ap * N + 4 * tid + e] = acc[ap * 4 + e];
         __syncthreads();
         ntt_inverse(arr, 4, N, itws, a.k, [](uint32_t x) { return x & 1u; });
         // CRT: x = x1 + p1 * ((x2 - x1) / p1 mod p2), signed, then mod 2^32
         uint32_t *dst = reinterpret_cast<uint32_t *>(a.out + (o - a.out_begin) * a.out_stride);
         const uint32_t bias = uint32_t(a.bias ? a.bias[o] : 0) * uint32_t(a.one);
-        for (uint32_t x = threadIdx.x; x < 2 * N; x += blockDim.x) {
+        for (uint32_t x = tid; x < 2 * N; x += blockDim.x) {
             const uint32_t pl = x / N, j = x % N;
             const uint32_t x1 = arr[(2 * pl) * N + j], x2 = arr[(2 * pl + 1) * N + j];
             const uint32_t x1m = x1 >= p1 ? x1 - p1 : x1;
@@ -289,6 +318,12 @@ __global__ void __launch_bounds__(kScoreThreads) k_intpoly_score(const IntpolyAr
             }
             dst[x] = w;
         }
+        __syncthreads();  // arr is read before the next output overwrites it
+    }
+    if (!ok && tid == 0) {
+        // a copy never landed: let every copy still in flight land before exiting
+        for (uint64_t k = consumed > 0 ? consumed - 1 : 0; k < issued; ++k)
+            mbar_wait_bounded(&full[k % kScoreStages], uint32_t((k / kScoreStages) & 1u), nullptr);
     }
 }
 
@@ -522,7 +557,12 @@ extern "C" idash_status idash_score_intpoly_device(idash_model *m, const void *d
     a.out = static_cast<uint8_t *>(d_out) + ol->payload_offset;
     a.out_stride = ol->row_stride;
     a.err = ctx->d_err;
-    const size_t smem = size_t(6) * ip.N * 4 + kRowStage * 4;
+    const size_t smem = 128 + (size_t(kScoreStages) * ip_stage_words(ip.N) + 6 * size_t(ip.N)) * 4;
+    // the ring needs more than the default 48 KiB of dynamic shared memory
+    if ((s = ctx->check_cuda(cudaFuncSetAttribute(k_intpoly_score, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                  int(smem)),
+                             "k_intpoly_score shared memory")) != IDASH_OK)
+        return s;
     // one wave of resident CTAs, each striding over the outputs
     int resident = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, k_intpoly_score, kScoreThreads, smem) != cudaSuccess ||
