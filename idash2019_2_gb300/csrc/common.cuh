@@ -59,12 +59,27 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
     return done != 0;
 }
 
+// As mbar_try_wait, but the thread may be suspended for up to `ns`
+// nanoseconds waiting for the phase (it resumes when the phase completes), so
+// a waiting warp does not spin through issue slots.
+__device__ __forceinline__ bool mbar_try_wait_sleep(uint64_t *bar, uint32_t parity, uint32_t ns) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"(smem_addr(bar)), "r"(parity), "r"(ns)
+        : "memory");
+    return done != 0;
+}
+
 // Waits for the barrier phase `parity` to complete, for at most
 // kWaitLimitCycles.  Returns false (and records kDevTimeout) on expiry.
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity, uint32_t *err) {
     if (mbar_try_wait(bar, parity)) return true;
     const long long t0 = clock64();
-    while (!mbar_try_wait(bar, parity)) {
+    while (!mbar_try_wait_sleep(bar, parity, 1000000u)) {
         if (clock64() - t0 > kWaitLimitCycles) {
             report_error(err, kDevTimeout);
             return false;
