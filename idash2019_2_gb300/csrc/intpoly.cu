@@ -19,6 +19,7 @@
 // output's terms, inverse NTT, CRT, epilogue).  Negacyclic NTTs are the
 // Cooley-Tukey / Gentleman-Sande pair with bit-reversed powers of a primitive
 // 2N-th root psi (Longa & Naehrig, CANS 2016).
+#include <algorithm>
 #include <cstring>
 #include <vector>
 
@@ -173,6 +174,8 @@ __global__ void __launch_bounds__(kNttThreads) k_ntt_rows(const uint8_t *in, uin
 struct IntpolyArgs {
     const uint64_t *term_ptr;
     const uint32_t *term_row;
+    const uint64_t *group_first;  // group g: outputs [group_first[g], group_first[g + 1])
+    uint64_t group_begin, group_end;  // groups scored by this launch
     const uint32_t *w_hat;
     const uint32_t *c_hat;
     const int32_t *bias;
@@ -180,40 +183,46 @@ struct IntpolyArgs {
     NttConsts k;
     uint32_t N, num_samples, region_size, n_rows;
     int32_t one;
-    uint64_t out_begin, out_end;
-    uint8_t *out;  // payload of output row 0 (output o -> row o - out_begin)
+    uint64_t out_begin, out_end;  // outputs written (output o -> row o - out_begin)
+    uint8_t *out;  // payload of output row 0
     uint64_t out_stride;
     uint32_t *err;
 };
 
 constexpr int kScoreThreads = 256;   // k_intpoly_score: thread x owns NTT points 4x..4x+3
-constexpr uint32_t kScoreStages = 3;  // terms in flight per CTA
+constexpr uint32_t kScoreStages = 4;  // row steps in flight per CTA
+constexpr uint32_t kGroupMax = 3;     // outputs sharing one term-row list (a target's genotypes)
 
 __device__ __forceinline__ void ip_mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
                  : "memory");
 }
 
-// Stage layout: one term's weight transform (2 primes x N words) then the
-// input row's transform (2 polynomials x 2 primes x N words).
-__host__ __device__ constexpr uint32_t ip_stage_words(uint32_t N) { return 6 * N; }
+// Stage layout: the input row's transform (2 polynomials x 2 primes x N
+// words), then the weight transforms (2 primes x N words) of up to kGroupMax
+// outputs at the same term position.
+__host__ __device__ constexpr uint32_t ip_stage_words(uint32_t N) { return (4 + 2 * kGroupMax) * N; }
+__host__ __device__ constexpr size_t ip_score_smem(uint32_t N) {
+    return 128 + (size_t(kScoreStages) * ip_stage_words(N) + 4 * size_t(kGroupMax) * N + 2 * size_t(N)) * 4;
+}
 
-// One CTA per output (grid-stride), a bulk-copy pipeline over the terms.
-// Thread 0 keeps kScoreStages terms in flight: each term's weight transform
-// (8 KiB) and input-row transform (16 KiB) are copied with cp.async.bulk into
-// a ring stage and completed on that stage's mbarrier; the CTA computes on the
-// oldest stage (thread x: NTT points 4x..4x+3 of the four arrays), agrees at a
-// barrier that the stage is free, and thread 0 refills it with the term
-// kScoreStages ahead, across output boundaries.  Then inverse NTT, CRT and
-// the a1 epilogue.  Every wait is bounded; a CTA whose copy never lands
-// drains its copies in flight and stops.
+// One CTA per output group (grid-stride): the outputs of a group read the
+// same input rows in the same order (normally the three genotype outputs of a
+// target), so each row step brings one input transform (16 KiB) and one
+// weight transform (8 KiB) per output.  Thread 0 keeps kScoreStages row steps
+// in flight with cp.async.bulk into a ring completed on mbarriers, across
+// group boundaries; the CTA computes on the oldest stage (thread x: NTT points
+// 4x..4x+3 of the group's arrays), agrees at a barrier that it is free, and
+// thread 0 refills it.  Then inverse NTTs, CRT and the a1 epilogue per
+// output.  Every wait is bounded; a CTA whose copy never lands drains its
+// copies in flight and stops.
 __global__ void __launch_bounds__(kScoreThreads) k_intpoly_score(const IntpolyArgs a) {
     extern __shared__ __align__(128) uint8_t ip_smem[];
     const uint32_t N = a.N;
-    uint64_t *full = reinterpret_cast<uint64_t *>(ip_smem);                     // [kScoreStages]
-    uint32_t *stage0 = reinterpret_cast<uint32_t *>(ip_smem + 128);             // kScoreStages x 6N
-    uint32_t *arr = stage0 + kScoreStages * ip_stage_words(N);                  // 4 arrays of N
-    uint32_t *itws = arr + 4 * N;                                               // 2N inverse twiddles
+    uint64_t *full = reinterpret_cast<uint64_t *>(ip_smem);             // [kScoreStages]
+    uint32_t *stage0 = reinterpret_cast<uint32_t *>(ip_smem + 128);     // kScoreStages x stage
+    uint32_t *arr = stage0 + kScoreStages * ip_stage_words(N);          // [output][poly][prime][N]
+    uint32_t *itws = arr + 4 * kGroupMax * N;                           // 2N inverse twiddles
     const uint32_t tid = threadIdx.x;
     if (tid == 0) {
         for (uint32_t s = 0; s < kScoreStages; ++s) mbar_init(&full[s], 1);
@@ -222,24 +231,30 @@ __global__ void __launch_bounds__(kScoreThreads) k_intpoly_score(const IntpolyAr
     for (uint32_t x = tid; x < 2 * N; x += blockDim.x) itws[x] = a.itw[x];
     __syncthreads();
 
-    // Fetch cursor (thread 0): the next (output, term) of this CTA's
-    // sequence, with that term's input row loaded one issue ahead so its
-    // latency hides behind a term's arithmetic.
-    uint64_t f_o = a.out_begin + blockIdx.x, f_t = 0, f_end = 0;
+    // Fetch cursor (thread 0): the next (group, row step) of this CTA, with
+    // the row of that step loaded one issue ahead.
+    uint64_t f_g = a.group_begin + blockIdx.x, f_i = 0, f_n = 0;
+    uint64_t f_w[kGroupMax] = {0, 0, 0};  // weight index of the group's first term, per member
+    uint32_t f_m = 0;                     // members of the group
     uint32_t pre_r = 0;
-    uint64_t issued = 0;  // terms issued so far (stage = index % kScoreStages)
+    uint64_t issued = 0;
+    auto open_group = [&]() {
+        const uint64_t o0 = a.group_first[f_g];
+        f_m = uint32_t(a.group_first[f_g + 1] - o0);
+#pragma unroll
+        for (uint32_t m = 0; m < kGroupMax; ++m) f_w[m] = m < f_m ? a.term_ptr[o0 + m] : 0;
+        f_i = 0;
+        f_n = a.term_ptr[o0 + 1] - f_w[0];
+    };
     auto advance = [&]() {
-        while (f_o < a.out_end && f_t >= f_end) {  // skip finished and empty outputs
-            f_o += gridDim.x;
-            if (f_o < a.out_end) {
-                f_t = a.term_ptr[f_o];
-                f_end = a.term_ptr[f_o + 1];
-            }
+        while (f_g < a.group_end && f_i >= f_n) {  // skip finished and empty groups
+            f_g += gridDim.x;
+            if (f_g < a.group_end) open_group();
         }
-        if (f_o < a.out_end) pre_r = a.term_row[f_t];
+        if (f_g < a.group_end) pre_r = a.term_row[f_w[0] + f_i];
     };
     auto issue_next = [&]() {
-        if (f_o >= a.out_end) return;
+        if (f_g >= a.group_end) return;
         uint32_t r = pre_r;
         if (r >= a.n_rows) {
             report_error(a.err, kDevBadIndex);
@@ -248,45 +263,61 @@ __global__ void __launch_bounds__(kScoreThreads) k_intpoly_score(const IntpolyAr
         const uint32_t s = uint32_t(issued % kScoreStages);
         uint32_t *st = stage0 + s * ip_stage_words(N);
         fence_proxy_async_smem();
-        ip_mbar_expect_tx(&full[s], 6 * N * 4);
-        bulk_g2s(st, a.w_hat + f_t * 2 * N, 2 * N * 4, &full[s]);
-        bulk_g2s(st + 2 * N, a.c_hat + uint64_t(r) * 4 * N, 4 * N * 4, &full[s]);
+        ip_mbar_expect_tx(&full[s], (4 + 2 * f_m) * N * 4);
+        bulk_g2s(st, a.c_hat + uint64_t(r) * 4 * N, 4 * N * 4, &full[s]);
+#pragma unroll
+        for (uint32_t m = 0; m < kGroupMax; ++m)
+            if (m < f_m) bulk_g2s(st + (4 + 2 * m) * N, a.w_hat + (f_w[m] + f_i) * 2 * N, 2 * N * 4, &full[s]);
         ++issued;
-        ++f_t;
+        ++f_i;
         advance();
     };
-    if (tid == 0 && f_o < a.out_end) {
-        f_t = a.term_ptr[f_o];
-        f_end = a.term_ptr[f_o + 1];
+    if (tid == 0 && f_g < a.group_end) {
+        open_group();
         advance();
-    }
-    if (tid == 0)
         for (uint32_t i = 0; i < kScoreStages; ++i) issue_next();
+    }
 
     const uint32_t p0 = a.k.p[0], p1 = a.k.p[1], i0 = a.k.pinv[0], i1 = a.k.pinv[1];
     uint64_t consumed = 0;
     bool ok = true;
-    for (uint64_t o = a.out_begin + blockIdx.x; o < a.out_end && ok; o += gridDim.x) {
-        uint32_t acc[16];  // [poly * 2 + prime][4]
+    for (uint64_t g = a.group_begin + blockIdx.x; g < a.group_end && ok; g += gridDim.x) {
+        const uint64_t o0 = a.group_first[g];
+        const uint32_t gm = uint32_t(a.group_first[g + 1] - o0);
+        const uint64_t nt = a.term_ptr[o0 + 1] - a.term_ptr[o0];
+        uint32_t acc[kGroupMax][16];  // [member][poly * 2 + prime][4]
 #pragma unroll
-        for (int e = 0; e < 16; ++e) acc[e] = 0;
-        const uint64_t nt = a.term_ptr[o + 1] - a.term_ptr[o];
+        for (uint32_t m = 0; m < kGroupMax; ++m)
+#pragma unroll
+            for (int e = 0; e < 16; ++e) acc[m][e] = 0;
         for (uint64_t i = 0; i < nt; ++i) {
             const uint32_t s = uint32_t(consumed % kScoreStages);
             const bool got = mbar_wait_bounded(&full[s], uint32_t((consumed / kScoreStages) & 1u), a.err);
             const uint32_t *st = stage0 + s * ip_stage_words(N);
-            const uint4 *wv = reinterpret_cast<const uint4 *>(st);
-            const uint4 *cv = reinterpret_cast<const uint4 *>(st + 2 * N);
-            const uint4 w0 = wv[tid], w1 = wv[N / 4 + tid];
-            const uint32_t W[2][4] = {{w0.x, w0.y, w0.z, w0.w}, {w1.x, w1.y, w1.z, w1.w}};
+            const uint4 *cv = reinterpret_cast<const uint4 *>(st);
+            uint32_t Cv[4][4];
 #pragma unroll
-            for (int ap = 0; ap < 4; ++ap) {  // (poly, prime)
+            for (int ap = 0; ap < 4; ++ap) {
                 const uint4 c = cv[ap * (N / 4) + tid];
-                const uint32_t Cv[4] = {c.x, c.y, c.z, c.w};
-                const int q = ap & 1;
-                const uint32_t p = q ? p1 : p0, pinv = q ? i1 : i0;
+                Cv[ap][0] = c.x;
+                Cv[ap][1] = c.y;
+                Cv[ap][2] = c.z;
+                Cv[ap][3] = c.w;
+            }
 #pragma unroll
-                for (int e = 0; e < 4; ++e) acc[ap * 4 + e] = mod_add(acc[ap * 4 + e], mont_mul(W[q][e], Cv[e], p, pinv), p);
+            for (uint32_t m = 0; m < kGroupMax; ++m) {
+                if (m >= gm) break;
+                const uint4 *wv = reinterpret_cast<const uint4 *>(st + (4 + 2 * m) * N);
+                const uint4 w0 = wv[tid], w1 = wv[N / 4 + tid];
+                const uint32_t W[2][4] = {{w0.x, w0.y, w0.z, w0.w}, {w1.x, w1.y, w1.z, w1.w}};
+#pragma unroll
+                for (int ap = 0; ap < 4; ++ap) {  // (poly, prime)
+                    const int q = ap & 1;
+                    const uint32_t p = q ? p1 : p0, pinv = q ? i1 : i0;
+#pragma unroll
+                    for (int e = 0; e < 4; ++e)
+                        acc[m][ap * 4 + e] = mod_add(acc[m][ap * 4 + e], mont_mul(W[q][e], Cv[ap][e], p, pinv), p);
+                }
             }
             ++consumed;
             // every thread is done with stage s (and agrees the copy landed)
@@ -296,29 +327,33 @@ __global__ void __launch_bounds__(kScoreThreads) k_intpoly_score(const IntpolyAr
         }
         if (!ok) break;
 #pragma unroll
-        for (int ap = 0; ap < 4; ++ap)
+        for (uint32_t m = 0; m < kGroupMax; ++m) {
+            if (m >= gm) break;
 #pragma unroll
-            for (int e = 0; e < 4; ++e) arr[ap * N + 4 * tid + e] = acc[ap * 4 + e];
+            for (int ap = 0; ap < 4; ++ap)
+#pragma unroll
+                for (int e = 0; e < 4; ++e) arr[(4 * m + ap) * N + 4 * tid + e] = acc[m][ap * 4 + e];
+        }
         __syncthreads();
-        ntt_inverse(arr, 4, N, itws, a.k, [](uint32_t x) { return x & 1u; });
+        ntt_inverse(arr, int(4 * gm), N, itws, a.k, [](uint32_t x) { return x & 1u; });
         // CRT: x = x1 + p1 * ((x2 - x1) / p1 mod p2), signed, then mod 2^32
-        uint32_t *dst = reinterpret_cast<uint32_t *>(a.out + (o - a.out_begin) * a.out_stride);
-        const uint32_t bias = uint32_t(a.bias ? a.bias[o] : 0) * uint32_t(a.one);
-        for (uint32_t x = tid; x < 2 * N; x += blockDim.x) {
-            const uint32_t pl = x / N, j = x % N;
-            const uint32_t x1 = arr[(2 * pl) * N + j], x2 = arr[(2 * pl + 1) * N + j];
+        for (uint32_t x = tid; x < 2 * N * gm; x += blockDim.x) {
+            const uint32_t m = x / (2 * N), pl = (x / N) % 2, j = x % N;
+            const uint64_t o = o0 + m;
+            if (o < a.out_begin || o >= a.out_end) continue;
+            const uint32_t x1 = arr[(4 * m + 2 * pl) * N + j], x2 = arr[(4 * m + 2 * pl + 1) * N + j];
             const uint32_t x1m = x1 >= p1 ? x1 - p1 : x1;
             const uint32_t t = mont_mul(mod_sub(x2, x1m, p1), a.k.p1inv_m, p1, i1);
             uint64_t v = uint64_t(x1) + uint64_t(p0) * t;
             uint32_t w = uint32_t(v);
             if (v > a.k.M_half) w -= uint32_t(a.k.M);
             if (pl == 1) {
-                if (j < a.num_samples) w += bias;
+                if (j < a.num_samples) w += uint32_t(a.bias ? a.bias[o] : 0) * uint32_t(a.one);
                 if (j >= a.region_size) w = 0;
             }
-            dst[x] = w;
+            reinterpret_cast<uint32_t *>(a.out + (o - a.out_begin) * a.out_stride)[pl * N + j] = w;
         }
-        __syncthreads();  // arr is read before the next output overwrites it
+        __syncthreads();  // arr is read before the next group overwrites it
     }
     if (!ok && tid == 0) {
         // a copy never landed: let every copy still in flight land before exiting
@@ -384,6 +419,10 @@ struct IntpolyModel {
     NttConsts k{};
     uint64_t *d_term_ptr = nullptr;
     uint32_t *d_term_row = nullptr;
+    // Output groups: consecutive outputs (at most kGroupMax) with identical
+    // term-row lists; group g is outputs [group_first[g], group_first[g + 1]).
+    std::vector<uint64_t> group_first;
+    uint64_t *d_group_first = nullptr;
     int32_t *d_bias = nullptr;
     uint32_t *d_w_hat = nullptr;
     uint32_t *d_tw = nullptr;   // forward twiddles [2][N]
@@ -393,6 +432,7 @@ struct IntpolyModel {
     ~IntpolyModel() {
         cudaFree(d_term_ptr);
         cudaFree(d_term_row);
+        cudaFree(d_group_first);
         cudaFree(d_bias);
         cudaFree(d_w_hat);
         cudaFree(d_tw);
@@ -465,6 +505,20 @@ extern "C" idash_status idash_model_intpoly(idash_ctx *ctx, idash_model **model,
         s = ctx->check_cuda(cudaMalloc(dst, std::max<size_t>(bytes, 16)), what);
         if (s == IDASH_OK && bytes) s = ctx->check_cuda(cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice), what);
     };
+    // groups of outputs that read the same rows in the same order
+    ip.group_first.clear();
+    for (uint64_t o = 0; o < n_out;) {
+        uint64_t e = o + 1;
+        const uint64_t len = term_ptr[o + 1] - term_ptr[o];
+        while (e < n_out && e - o < kGroupMax && term_ptr[e + 1] - term_ptr[e] == len &&
+               std::equal(term_feat + term_ptr[o], term_feat + term_ptr[o + 1], term_feat + term_ptr[e]))
+            ++e;
+        ip.group_first.push_back(o);
+        o = e;
+    }
+    ip.group_first.push_back(n_out);
+    up(reinterpret_cast<void **>(&ip.d_group_first), ip.group_first.data(), ip.group_first.size() * 8,
+       "intpoly groups");
     up(reinterpret_cast<void **>(&ip.d_term_ptr), term_ptr, (n_out + 1) * 8, "intpoly term_ptr");
     up(reinterpret_cast<void **>(&ip.d_term_row), term_feat, nnz * 4, "intpoly term rows");
     up(reinterpret_cast<void **>(&ip.d_bias), bias_v.data(), n_out * 4, "intpoly bias");
@@ -542,6 +596,13 @@ extern "C" idash_status idash_score_intpoly_device(idash_model *m, const void *d
     IntpolyArgs a{};
     a.term_ptr = ip.d_term_ptr;
     a.term_row = ip.d_term_row;
+    a.group_first = ip.d_group_first;
+    {
+        // groups holding outputs of [out_begin, out_end)
+        const auto &G = ip.group_first;
+        a.group_begin = uint64_t(std::upper_bound(G.begin(), G.end() - 1, out_begin) - G.begin()) - 1;
+        a.group_end = uint64_t(std::lower_bound(G.begin(), G.end() - 1, out_end) - G.begin());
+    }
     a.w_hat = ip.d_w_hat;
     a.c_hat = ip.d_c_hat;
     a.bias = ip.d_bias;
@@ -557,19 +618,19 @@ extern "C" idash_status idash_score_intpoly_device(idash_model *m, const void *d
     a.out = static_cast<uint8_t *>(d_out) + ol->payload_offset;
     a.out_stride = ol->row_stride;
     a.err = ctx->d_err;
-    const size_t smem = 128 + (size_t(kScoreStages) * ip_stage_words(ip.N) + 6 * size_t(ip.N)) * 4;
+    const size_t smem = ip_score_smem(ip.N);
     // the ring needs more than the default 48 KiB of dynamic shared memory
     if ((s = ctx->check_cuda(cudaFuncSetAttribute(k_intpoly_score, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                   int(smem)),
                              "k_intpoly_score shared memory")) != IDASH_OK)
         return s;
-    // one wave of resident CTAs, each striding over the outputs
+    // one wave of resident CTAs, each striding over the groups
     int resident = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, k_intpoly_score, kScoreThreads, smem) != cudaSuccess ||
         resident < 1)
         resident = 1;
-    const uint32_t grid =
-        uint32_t(std::min<uint64_t>(out_end - out_begin, uint64_t(ctx->sm_count) * uint64_t(resident)));
+    const uint32_t grid = uint32_t(
+        std::min<uint64_t>(a.group_end - a.group_begin, uint64_t(ctx->sm_count) * uint64_t(resident)));
     k_intpoly_score<<<grid, kScoreThreads, smem, st>>>(a);
     s = ctx->check_cuda(cudaGetLastError(), "k_intpoly_score launch");
     if (s == IDASH_OK) ctx->stats.kernel_launches += 2;

@@ -46,6 +46,37 @@ def test_intpoly_matches_schoolbook(ctx, oracle, seed, n_out, max_terms, ns, rs)
     m.free()
 
 
+def test_intpoly_output_groups_and_ranges(ctx, oracle):
+    """Outputs that read the same rows in the same order (a target's three
+    genotype models) are scored together; groups of 3, 2 and 1, an empty
+    output, and ranges that cut groups in the middle all stay exact."""
+    rng = np.random.default_rng(7)
+    n_rows, lists = 30, []
+    for size in (3, 1, 2, 3, 3, 1, 3):
+        rows_of = rng.integers(0, n_rows, size=int(rng.integers(1, 25))).astype(np.uint32)
+        lists += [rows_of] * size
+    lists[4] = np.zeros(0, np.uint32)  # an output with no terms inside a would-be group
+    ptr = np.concatenate([[0], np.cumsum([len(x) for x in lists])]).astype(np.uint64)
+    feat = np.concatenate(lists).astype(np.uint32)
+    poly = rng.integers(-8192, 8192, size=(len(feat), 1024)).astype(np.int16)
+    rows = rng.integers(0, 2 ** 32, size=(n_rows, 2048), dtype=np.uint64).astype(np.uint32).view(np.int32)
+    bias = rng.integers(-8192, 8192, size=len(lists)).astype(np.int32)
+    n_out = len(lists)
+    csr = gpu.CSRModel(ptr, feat, np.zeros(len(feat), np.int32))
+    m = gpu.IntpolyModel(ctx, csr, poly, n_rows, 1000, 1024, bias=bias)
+    want = oracle.intpoly_score(ptr, feat, poly, bias, rows, 1000, 1024, 0, n_out)
+    d_in = ctx.device_alloc(rows.nbytes)
+    d_in.upload(rows)
+    for lo, hi in [(0, n_out), (1, 8), (4, 5), (5, n_out), (n_out - 1, n_out)]:
+        d_out = ctx.device_alloc((hi - lo) * 8192)
+        m.score_device(d_in.ptr, gpu.DENSE_TRLWE, lo, hi, d_out.ptr, gpu.DENSE_TRLWE)
+        ctx.sync()
+        np.testing.assert_array_equal(d_out.download(dtype=np.int32).reshape(hi - lo, 2048), want[lo:hi])
+        d_out.free()
+    d_in.free()
+    m.free()
+
+
 def test_constant_polynomials_equal_the_trlwe_form(ctx):
     """With every weight a constant polynomial, the product is the reference's
     tLweAddMulTo sum: the two kernels agree."""
