@@ -189,9 +189,9 @@ struct IntpolyArgs {
     uint32_t *err;
 };
 
-constexpr int kScoreThreads = 256;   // k_intpoly_score: thread x owns NTT points 4x..4x+3
-constexpr uint32_t kScoreStages = 4;  // row steps in flight per CTA
 constexpr uint32_t kGroupMax = 3;     // outputs sharing one term-row list (a target's genotypes)
+constexpr int kScoreThreads = 256 * kGroupMax;  // k_intpoly_score: 256 threads per group member
+constexpr uint32_t kScoreStages = 4;  // row steps in flight per CTA
 
 __device__ __forceinline__ void ip_mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
@@ -211,9 +211,9 @@ __host__ __device__ constexpr size_t ip_score_smem(uint32_t N) {
 // target), so each row step brings one input transform (16 KiB) and one
 // weight transform (8 KiB) per output.  Thread 0 keeps kScoreStages row steps
 // in flight with cp.async.bulk into a ring completed on mbarriers, across
-// group boundaries; the CTA computes on the oldest stage (thread x: NTT points
-// 4x..4x+3 of the group's arrays), agrees at a barrier that it is free, and
-// thread 0 refills it.  Then inverse NTTs, CRT and the a1 epilogue per
+// group boundaries; the CTA computes on the oldest stage (thread x: group
+// member x / 256, NTT points 4q..4q+3 of its four arrays, q = x % 256),
+// agrees at a barrier that it is free, and thread 0 refills it.  Then inverse NTTs, CRT and the a1 epilogue per
 // output.  Every wait is bounded; a CTA whose copy never lands drains its
 // copies in flight and stops.
 __global__ void __launch_bounds__(kScoreThreads) k_intpoly_score(const IntpolyArgs a) {
@@ -285,38 +285,29 @@ __global__ void __launch_bounds__(kScoreThreads) k_intpoly_score(const IntpolyAr
         const uint64_t o0 = a.group_first[g];
         const uint32_t gm = uint32_t(a.group_first[g + 1] - o0);
         const uint64_t nt = a.term_ptr[o0 + 1] - a.term_ptr[o0];
-        uint32_t acc[kGroupMax][16];  // [member][poly * 2 + prime][4]
+        const uint32_t me = tid >> 8, q4 = tid & 255u;  // group member, point quad
+        const bool active = me < gm;
+        uint32_t acc[16];  // [poly * 2 + prime][4]
 #pragma unroll
-        for (uint32_t m = 0; m < kGroupMax; ++m)
-#pragma unroll
-            for (int e = 0; e < 16; ++e) acc[m][e] = 0;
+        for (int e = 0; e < 16; ++e) acc[e] = 0;
         for (uint64_t i = 0; i < nt; ++i) {
             const uint32_t s = uint32_t(consumed % kScoreStages);
             const bool got = mbar_wait_bounded(&full[s], uint32_t((consumed / kScoreStages) & 1u), a.err);
-            const uint32_t *st = stage0 + s * ip_stage_words(N);
-            const uint4 *cv = reinterpret_cast<const uint4 *>(st);
-            uint32_t Cv[4][4];
-#pragma unroll
-            for (int ap = 0; ap < 4; ++ap) {
-                const uint4 c = cv[ap * (N / 4) + tid];
-                Cv[ap][0] = c.x;
-                Cv[ap][1] = c.y;
-                Cv[ap][2] = c.z;
-                Cv[ap][3] = c.w;
-            }
-#pragma unroll
-            for (uint32_t m = 0; m < kGroupMax; ++m) {
-                if (m >= gm) break;
-                const uint4 *wv = reinterpret_cast<const uint4 *>(st + (4 + 2 * m) * N);
-                const uint4 w0 = wv[tid], w1 = wv[N / 4 + tid];
+            if (active) {
+                const uint32_t *st = stage0 + s * ip_stage_words(N);
+                const uint4 *cv = reinterpret_cast<const uint4 *>(st);
+                const uint4 *wv = reinterpret_cast<const uint4 *>(st + (4 + 2 * me) * N);
+                const uint4 w0 = wv[q4], w1 = wv[N / 4 + q4];
                 const uint32_t W[2][4] = {{w0.x, w0.y, w0.z, w0.w}, {w1.x, w1.y, w1.z, w1.w}};
 #pragma unroll
                 for (int ap = 0; ap < 4; ++ap) {  // (poly, prime)
+                    const uint4 c = cv[ap * (N / 4) + q4];
+                    const uint32_t Cv[4] = {c.x, c.y, c.z, c.w};
                     const int q = ap & 1;
                     const uint32_t p = q ? p1 : p0, pinv = q ? i1 : i0;
 #pragma unroll
                     for (int e = 0; e < 4; ++e)
-                        acc[m][ap * 4 + e] = mod_add(acc[m][ap * 4 + e], mont_mul(W[q][e], Cv[ap][e], p, pinv), p);
+                        acc[ap * 4 + e] = mod_add(acc[ap * 4 + e], mont_mul(W[q][e], Cv[e], p, pinv), p);
                 }
             }
             ++consumed;
@@ -326,13 +317,11 @@ __global__ void __launch_bounds__(kScoreThreads) k_intpoly_score(const IntpolyAr
             if (tid == 0) issue_next();
         }
         if (!ok) break;
-#pragma unroll
-        for (uint32_t m = 0; m < kGroupMax; ++m) {
-            if (m >= gm) break;
+        if (active) {
 #pragma unroll
             for (int ap = 0; ap < 4; ++ap)
 #pragma unroll
-                for (int e = 0; e < 4; ++e) arr[(4 * m + ap) * N + 4 * tid + e] = acc[m][ap * 4 + e];
+                for (int e = 0; e < 4; ++e) arr[(4 * me + ap) * N + 4 * q4 + e] = acc[ap * 4 + e];
         }
         __syncthreads();
         ntt_inverse(arr, int(4 * gm), N, itws, a.k, [](uint32_t x) { return x & 1u; });
