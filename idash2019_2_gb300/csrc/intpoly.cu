@@ -193,6 +193,14 @@ constexpr uint32_t kGroupMax = 3;     // outputs sharing one term-row list (a ta
 constexpr int kScoreThreads = 256 * kGroupMax;  // k_intpoly_score: 256 threads per group member
 constexpr uint32_t kScoreStages = 4;  // row steps in flight per CTA
 
+// Montgomery reduction without the final correction: a value in [0, 2p)
+// congruent to a*b*2^-32 mod p (a, b < p < 2^31).
+__device__ __forceinline__ uint32_t mont_mul_lazy(uint32_t a, uint32_t b, uint32_t p, uint32_t pinv) {
+    const uint64_t t = uint64_t(a) * b;
+    const uint32_t m = uint32_t(t) * pinv;
+    return uint32_t((t + uint64_t(m) * p) >> 32);
+}
+
 __device__ __forceinline__ void ip_mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
                  : "memory");
@@ -287,7 +295,9 @@ __global__ void __launch_bounds__(kScoreThreads) k_intpoly_score(const IntpolyAr
         const uint64_t nt = a.term_ptr[o0 + 1] - a.term_ptr[o0];
         const uint32_t me = tid >> 8, q4 = tid & 255u;  // group member, point quad
         const bool active = me < gm;
-        uint32_t acc[16];  // [poly * 2 + prime][4]
+        // unreduced sums of lazy Montgomery products (each < 2p, so a sum of
+        // fewer than 2^31 terms fits 64 bits), reduced once after the terms
+        uint64_t acc[16];  // [poly * 2 + prime][4]
 #pragma unroll
         for (int e = 0; e < 16; ++e) acc[e] = 0;
         for (uint64_t i = 0; i < nt; ++i) {
@@ -306,8 +316,7 @@ __global__ void __launch_bounds__(kScoreThreads) k_intpoly_score(const IntpolyAr
                     const int q = ap & 1;
                     const uint32_t p = q ? p1 : p0, pinv = q ? i1 : i0;
 #pragma unroll
-                    for (int e = 0; e < 4; ++e)
-                        acc[ap * 4 + e] = mod_add(acc[ap * 4 + e], mont_mul(W[q][e], Cv[e], p, pinv), p);
+                    for (int e = 0; e < 4; ++e) acc[ap * 4 + e] += mont_mul_lazy(W[q][e], Cv[e], p, pinv);
                 }
             }
             ++consumed;
@@ -319,9 +328,20 @@ __global__ void __launch_bounds__(kScoreThreads) k_intpoly_score(const IntpolyAr
         if (!ok) break;
         if (active) {
 #pragma unroll
-            for (int ap = 0; ap < 4; ++ap)
+            for (int ap = 0; ap < 4; ++ap) {
+                const int q = ap & 1;
+                const uint32_t p = q ? p1 : p0, pinv = q ? i1 : i0;
 #pragma unroll
-                for (int e = 0; e < 4; ++e) arr[(4 * me + ap) * N + 4 * q4 + e] = acc[ap * 4 + e];
+                for (int e = 0; e < 4; ++e) {
+                    // REDC of the 64-bit sum T (< p * 2^32): u = T * 2^-32 mod p,
+                    // then * 2^64 * 2^-32 (Montgomery product with R^2) gives T mod p
+                    const uint64_t T = acc[ap * 4 + e];
+                    const uint32_t m = uint32_t(T) * pinv;
+                    uint32_t u = uint32_t((T + uint64_t(m) * p) >> 32);
+                    u = u >= p ? u - p : u;
+                    arr[(4 * me + ap) * N + 4 * q4 + e] = mont_mul(u, a.k.r2[q], p, pinv);
+                }
+            }
         }
         __syncthreads();
         ntt_inverse(arr, int(4 * gm), N, itws, a.k, [](uint32_t x) { return x & 1u; });
