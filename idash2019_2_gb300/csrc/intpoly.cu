@@ -191,7 +191,8 @@ struct IntpolyArgs {
 
 constexpr uint32_t kGroupMax = 3;     // outputs sharing one term-row list (a target's genotypes)
 constexpr int kScoreThreads = 256 * kGroupMax;  // k_intpoly_score: 256 threads per group member
-constexpr uint32_t kScoreStages = 4;  // row steps in flight per CTA
+constexpr uint32_t kScoreStages = 4;     // row steps in flight per CTA
+constexpr uint32_t kScoreStepTerms = 2;  // row steps consumed per CTA barrier
 
 // Montgomery reduction without the final correction: a value in [0, 2p)
 // congruent to a*b*2^-32 mod p (a, b < p < 2^31).
@@ -300,30 +301,37 @@ __global__ void __launch_bounds__(kScoreThreads) k_intpoly_score(const IntpolyAr
         uint64_t acc[16];  // [poly * 2 + prime][4]
 #pragma unroll
         for (int e = 0; e < 16; ++e) acc[e] = 0;
-        for (uint64_t i = 0; i < nt; ++i) {
-            const uint32_t s = uint32_t(consumed % kScoreStages);
-            const bool got = mbar_wait_bounded(&full[s], uint32_t((consumed / kScoreStages) & 1u), a.err);
-            if (active) {
-                const uint32_t *st = stage0 + s * ip_stage_words(N);
-                const uint4 *cv = reinterpret_cast<const uint4 *>(st);
-                const uint4 *wv = reinterpret_cast<const uint4 *>(st + (4 + 2 * me) * N);
-                const uint4 w0 = wv[q4], w1 = wv[N / 4 + q4];
-                const uint32_t W[2][4] = {{w0.x, w0.y, w0.z, w0.w}, {w1.x, w1.y, w1.z, w1.w}};
+        // kScoreStepTerms row steps per barrier: the stages they used are
+        // refilled together after it
+        for (uint64_t i = 0; i < nt; i += kScoreStepTerms) {
+            const uint32_t steps = nt - i < kScoreStepTerms ? uint32_t(nt - i) : kScoreStepTerms;
+            bool got = true;
+            for (uint32_t d = 0; d < steps; ++d) {
+                const uint32_t s = uint32_t(consumed % kScoreStages);
+                got = mbar_wait_bounded(&full[s], uint32_t((consumed / kScoreStages) & 1u), a.err) && got;
+                if (active) {
+                    const uint32_t *st = stage0 + s * ip_stage_words(N);
+                    const uint4 *cv = reinterpret_cast<const uint4 *>(st);
+                    const uint4 *wv = reinterpret_cast<const uint4 *>(st + (4 + 2 * me) * N);
+                    const uint4 w0 = wv[q4], w1 = wv[N / 4 + q4];
+                    const uint32_t W[2][4] = {{w0.x, w0.y, w0.z, w0.w}, {w1.x, w1.y, w1.z, w1.w}};
 #pragma unroll
-                for (int ap = 0; ap < 4; ++ap) {  // (poly, prime)
-                    const uint4 c = cv[ap * (N / 4) + q4];
-                    const uint32_t Cv[4] = {c.x, c.y, c.z, c.w};
-                    const int q = ap & 1;
-                    const uint32_t p = q ? p1 : p0, pinv = q ? i1 : i0;
+                    for (int ap = 0; ap < 4; ++ap) {  // (poly, prime)
+                        const uint4 c = cv[ap * (N / 4) + q4];
+                        const uint32_t Cv[4] = {c.x, c.y, c.z, c.w};
+                        const int q = ap & 1;
+                        const uint32_t p = q ? p1 : p0, pinv = q ? i1 : i0;
 #pragma unroll
-                    for (int e = 0; e < 4; ++e) acc[ap * 4 + e] += mont_mul_lazy(W[q][e], Cv[e], p, pinv);
+                        for (int e = 0; e < 4; ++e) acc[ap * 4 + e] += mont_mul_lazy(W[q][e], Cv[e], p, pinv);
+                    }
                 }
+                ++consumed;
             }
-            ++consumed;
-            // every thread is done with stage s (and agrees the copy landed)
+            // every thread is done with these stages (and agrees the copies landed)
             ok = __syncthreads_and(got ? 1 : 0) != 0;
             if (!ok) break;
-            if (tid == 0) issue_next();
+            if (tid == 0)
+                for (uint32_t d = 0; d < steps; ++d) issue_next();
         }
         if (!ok) break;
         if (active) {
@@ -366,7 +374,7 @@ __global__ void __launch_bounds__(kScoreThreads) k_intpoly_score(const IntpolyAr
     }
     if (!ok && tid == 0) {
         // a copy never landed: let every copy still in flight land before exiting
-        for (uint64_t k = consumed > 0 ? consumed - 1 : 0; k < issued; ++k)
+        for (uint64_t k = consumed > kScoreStepTerms ? consumed - kScoreStepTerms : 0; k < issued; ++k)
             mbar_wait_bounded(&full[k % kScoreStages], uint32_t((k / kScoreStages) & 1u), nullptr);
     }
 }
