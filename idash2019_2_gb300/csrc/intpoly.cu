@@ -13,10 +13,11 @@
 // checked when the model is built.  S is computed modulo two NTT primes
 // p1, p2 < 2^31 (p = 1 mod 2N) and recovered by CRT, then reduced mod 2^32.
 //
-// Kernels: k_ntt_model (model polynomials -> Montgomery-form NTT, once per
-// model), k_ntt_rows (input TRLWE rows -> NTT, once per call) and
-// k_intpoly_score (one CTA per output: pointwise multiply-accumulate over the
-// output's terms, inverse NTT, CRT, epilogue).  Negacyclic NTTs are the
+// Kernels: k_ntt_model (model polynomials -> NTT, once per model), k_ntt_rows
+// (input TRLWE rows -> NTT, once per call), both stored as centred residues,
+// and k_intpoly_score (one CTA per group of outputs: pointwise
+// multiply-accumulate over the terms as exact 64-bit sums, inverse NTT, CRT,
+// epilogue).  Negacyclic NTTs are the
 // Cooley-Tukey / Gentleman-Sande pair with bit-reversed powers of a primitive
 // 2N-th root psi (Longa & Naehrig, CANS 2016).
 #include <algorithm>
@@ -34,13 +35,19 @@ constexpr uint32_t kPrimes[2] = {2147473409u, 2147389441u};  // both = 1 mod 204
 constexpr uint32_t kPsi2048[2] = {383167813u, 211808905u};   // primitive 2048-th roots of unity
 constexpr int kNttThreads = 256;
 
+// 2^32 mod p is small for both primes (20478 and 188414), so folding the high
+// word of a 64-bit sum onto the low one with it shrinks the sum below 2^49.
+static_assert((uint64_t(1) << 32) % kPrimes[0] < (1u << 18) && (uint64_t(1) << 32) % kPrimes[1] < (1u << 18),
+              "fold bound");
+
 struct NttConsts {
     uint32_t p[2];
-    uint32_t pinv[2];    // -p^-1 mod 2^32
-    uint32_t r2[2];      // R^2 mod p, R = 2^32
-    uint32_t ninv[2];    // N^-1 * R mod p
-    uint32_t p1inv_m;    // p1^-1 * R mod p2
-    uint64_t M, M_half;  // p1 * p2 and floor(M / 2)
+    uint32_t pinv[2];       // -p^-1 mod 2^32
+    int32_t r1[2];          // R mod p, R = 2^32
+    uint32_t nscale[2];     // N^-1 * R^2 mod p: Montgomery factor of the last inverse stage
+    uint32_t nscale_tw[2];  // nscale * (that stage's twiddle) mod p
+    uint32_t p1inv_m;       // p1^-1 * R mod p2
+    uint64_t M, M_half;     // p1 * p2 and floor(M / 2)
 };
 
 uint64_t mulmod(uint64_t a, uint64_t b, uint64_t p) { return uint64_t((unsigned __int128)a * b % p); }
@@ -71,17 +78,22 @@ __device__ __forceinline__ uint32_t residue(int32_t v, uint32_t p) {
     return uint32_t(x < 0 ? x + p : x);
 }
 
-// In-place negacyclic NTTs of `narr` arrays of length N in shared memory;
-// array i uses prime prime_of(i) and its twiddles tw[prime][N].
+// A residue x in [0, p) as the congruent value in (-p/2, p/2]: transforms are
+// stored this way so that a product of two has magnitude below 2^60.
+__device__ __forceinline__ int32_t centred(uint32_t x, uint32_t p) { return x > p / 2 ? int32_t(x - p) : int32_t(x); }
+
+// In-place negacyclic NTTs (Cooley-Tukey) of `narr` arrays of length N = 2^logn
+// in shared memory; array i uses prime prime_of(i) and its twiddles tw[prime][N].
 template <typename PrimeOf>
-__device__ void ntt_forward(uint32_t *arr, int narr, uint32_t N, const uint32_t *tw, const NttConsts &k,
+__device__ void ntt_forward(uint32_t *arr, int narr, uint32_t logn, const uint32_t *tw, const NttConsts &k,
                             PrimeOf prime_of) {
-    const uint32_t half = N / 2;
-    for (uint32_t m = 1, t = half; m < N; m <<= 1, t >>= 1) {
+    const uint32_t N = 1u << logn, half = N / 2;
+    for (uint32_t m = 1, lt = logn - 1; m < N; m <<= 1, --lt) {  // butterfly span t = 2^lt
+        const uint32_t t = 1u << lt;
         for (uint32_t x = threadIdx.x; x < half * narr; x += blockDim.x) {
-            const uint32_t a = x / half, b = x % half;
+            const uint32_t a = x >> (logn - 1), b = x & (half - 1);
             const uint32_t q = prime_of(a);
-            const uint32_t i = b / t, j = 2 * i * t + b % t;
+            const uint32_t i = b >> lt, j = (i << (lt + 1)) + (b & (t - 1));
             uint32_t *v = arr + a * N;
             const uint32_t S = tw[q * N + m + i];
             const uint32_t U = v[j], V = mont_mul(v[j + t], S, k.p[q], k.pinv[q]);
@@ -92,31 +104,14 @@ __device__ void ntt_forward(uint32_t *arr, int narr, uint32_t N, const uint32_t 
     }
 }
 
-template <typename PrimeOf>
-__device__ void ntt_inverse(uint32_t *arr, int narr, uint32_t N, const uint32_t *itw, const NttConsts &k,
-                            PrimeOf prime_of) {
-    const uint32_t half = N / 2;
-    for (uint32_t h = half, t = 1; h >= 1; h >>= 1, t <<= 1) {
-        for (uint32_t x = threadIdx.x; x < half * narr; x += blockDim.x) {
-            const uint32_t a = x / half, b = x % half;
-            const uint32_t q = prime_of(a);
-            const uint32_t i = b / t, j = 2 * i * t + b % t;
-            uint32_t *v = arr + a * N;
-            const uint32_t S = itw[q * N + h + i];
-            const uint32_t U = v[j], V = v[j + t];
-            v[j] = mod_add(U, V, k.p[q]);
-            v[j + t] = mont_mul(mod_sub(U, V, k.p[q]), S, k.p[q], k.pinv[q]);
-        }
-        __syncthreads();
-    }
-    for (uint32_t x = threadIdx.x; x < N * narr; x += blockDim.x) {
-        const uint32_t q = prime_of(x / N);
-        arr[x] = mont_mul(arr[x], k.ninv[q], k.p[q], k.pinv[q]);
-    }
-    __syncthreads();
+// Gentleman-Sande butterfly of the inverse transform: (u, v) -> (u + v, (u - v) * S).
+__device__ __forceinline__ void gs_butterfly(uint32_t &u, uint32_t &v, uint32_t S, uint32_t p, uint32_t pinv) {
+    const uint32_t d = mod_sub(u, v, p);
+    u = mod_add(u, v, p);
+    v = mont_mul(d, S, p, pinv);
 }
 
-// Model polynomials (int16, [term][N]) -> Montgomery-form NTT, [term][prime][N].
+// Model polynomials (int16, [term][N]) -> NTT, centred residues, [term][prime][N].
 // Coefficients beyond max_abs break the exactness bound: reported, not used.
 __global__ void __launch_bounds__(kNttThreads) k_ntt_model(const int16_t *w, uint64_t n_terms, uint32_t N,
                                                            const uint32_t *tw, NttConsts k, int32_t max_abs,
@@ -135,17 +130,16 @@ __global__ void __launch_bounds__(kNttThreads) k_ntt_model(const int16_t *w, uin
             arr[N + x] = residue(v, k.p[1]);
         }
         __syncthreads();
-        ntt_forward(arr, 2, N, tws, k, [](uint32_t a) { return a; });
+        ntt_forward(arr, 2, uint32_t(__ffs(N) - 1), tws, k, [](uint32_t a) { return a; });
         uint32_t *dst = w_hat + t * 2 * N;
         for (uint32_t x = threadIdx.x; x < 2 * N; x += blockDim.x) {
-            const uint32_t q = x / N;
-            dst[x] = mont_mul(arr[x], k.r2[q], k.p[q], k.pinv[q]);
+            dst[x] = uint32_t(centred(arr[x], k.p[x / N]));
         }
         __syncthreads();
     }
 }
 
-// Input TRLWE rows (a | b, signed words) -> NTT, [row][poly][prime][N].
+// Input TRLWE rows (a | b, signed words) -> NTT, centred residues, [row][poly][prime][N].
 __global__ void __launch_bounds__(kNttThreads) k_ntt_rows(const uint8_t *in, uint64_t stride, uint64_t n_rows,
                                                           uint32_t N, const uint32_t *tw, NttConsts k,
                                                           uint32_t *c_hat) {
@@ -163,10 +157,15 @@ __global__ void __launch_bounds__(kNttThreads) k_ntt_rows(const uint8_t *in, uin
             arr[(2 * poly + 1) * N + j] = residue(v, k.p[1]);
         }
         __syncthreads();
-        ntt_forward(arr, 4, N, tws, k, [](uint32_t a) { return a & 1u; });
+        ntt_forward(arr, 4, uint32_t(__ffs(N) - 1), tws, k, [](uint32_t a) { return a & 1u; });
         uint4 *dst = reinterpret_cast<uint4 *>(c_hat + r * 4 * N);
         const uint4 *s4 = reinterpret_cast<const uint4 *>(arr);
-        for (uint32_t x = threadIdx.x; x < N; x += blockDim.x) dst[x] = s4[x];
+        for (uint32_t x = threadIdx.x; x < N; x += blockDim.x) {
+            const uint32_t p = k.p[(4 * x / N) & 1u];  // 4 words of one (poly, prime) array
+            const uint4 v = s4[x];
+            dst[x] = make_uint4(uint32_t(centred(v.x, p)), uint32_t(centred(v.y, p)), uint32_t(centred(v.z, p)),
+                                uint32_t(centred(v.w, p)));
+        }
         __syncthreads();
     }
 }
@@ -189,17 +188,33 @@ struct IntpolyArgs {
     uint32_t *err;
 };
 
+constexpr uint32_t kIpN = 1024;      // polynomial size of the scoring kernel: 256 threads x 4 points
 constexpr uint32_t kGroupMax = 3;     // outputs sharing one term-row list (a target's genotypes)
 constexpr int kScoreThreads = 256 * kGroupMax;  // k_intpoly_score: 256 threads per group member
 constexpr uint32_t kScoreStages = 4;     // row steps in flight per CTA
 constexpr uint32_t kScoreStepTerms = 1;  // row steps consumed per CTA barrier (2 measured slower)
+// Products of centred residues have magnitude below 2^60; a folded sum is
+// below 2^49, so kFoldSteps products more stay below 2^63.
+constexpr uint32_t kFoldSteps = 7;
 
-// Montgomery reduction without the final correction: a value in [0, 2p)
-// congruent to a*b*2^-32 mod p (a, b < p < 2^31).
-__device__ __forceinline__ uint32_t mont_mul_lazy(uint32_t a, uint32_t b, uint32_t p, uint32_t pinv) {
-    const uint64_t t = uint64_t(a) * b;
-    const uint32_t m = uint32_t(t) * pinv;
-    return uint32_t((t + uint64_t(m) * p) >> 32);
+// c + a * b with a 64-bit result: one widening multiply-add.
+__device__ __forceinline__ int64_t mad_wide(int32_t a, int32_t b, int64_t c) {
+    int64_t d;
+    asm("mad.wide.s32 %0, %1, %2, %3;" : "=l"(d) : "r"(a), "r"(b), "l"(c));
+    return d;
+}
+
+// hi * 2^32 + lo  ->  hi * (2^32 mod p) + lo: same residue, magnitude < 2^49
+// for |T| < 2^63.
+__device__ __forceinline__ int64_t fold(int64_t T, int32_t r1) {
+    int64_t d;
+    asm("{\n\t.reg .b32 lo, hi;\n\t.reg .b64 z;\n\t"
+        "mov.b64 {lo, hi}, %1;\n\t"
+        "mov.b64 z, {lo, 0};\n\t"
+        "mad.wide.s32 %0, hi, %2, z;\n\t}"
+        : "=l"(d)
+        : "l"(T), "r"(r1));
+    return d;
 }
 
 __device__ __forceinline__ void ip_mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
@@ -222,12 +237,15 @@ __host__ __device__ constexpr size_t ip_score_smem(uint32_t N) {
 // in flight with cp.async.bulk into a ring completed on mbarriers, across
 // group boundaries; the CTA computes on the oldest stage (thread x: group
 // member x / 256, NTT points 4q..4q+3 of its four arrays, q = x % 256),
-// agrees at a barrier that it is free, and thread 0 refills it.  Then inverse NTTs, CRT and the a1 epilogue per
-// output.  Every wait is bounded; a CTA whose copy never lands drains its
-// copies in flight and stops.
+// agrees at a barrier that it is free, and thread 0 refills it.  A product
+// is one signed widening multiply-add into a 64-bit sum; every kFoldSteps
+// terms the sums are folded with 2^32 mod p, which keeps them exact without
+// a Montgomery reduction per product.  Then inverse NTTs, CRT and the a1
+// epilogue per output.  Every wait is bounded; a CTA whose copy never lands
+// drains its copies in flight and stops.
 __global__ void __launch_bounds__(kScoreThreads) k_intpoly_score(const IntpolyArgs a) {
     extern __shared__ __align__(128) uint8_t ip_smem[];
-    const uint32_t N = a.N;
+    constexpr uint32_t N = kIpN;  // a.N, checked on the host
     uint64_t *full = reinterpret_cast<uint64_t *>(ip_smem);             // [kScoreStages]
     uint32_t *stage0 = reinterpret_cast<uint32_t *>(ip_smem + 128);     // kScoreStages x stage
     uint32_t *arr = stage0 + kScoreStages * ip_stage_words(N);          // [output][poly][prime][N]
@@ -288,6 +306,7 @@ __global__ void __launch_bounds__(kScoreThreads) k_intpoly_score(const IntpolyAr
     }
 
     const uint32_t p0 = a.k.p[0], p1 = a.k.p[1], i0 = a.k.pinv[0], i1 = a.k.pinv[1];
+    const int32_t f0 = a.k.r1[0], f1 = a.k.r1[1];
     uint64_t consumed = 0;
     bool ok = true;
     for (uint64_t g = a.group_begin + blockIdx.x; g < a.group_end && ok; g += gridDim.x) {
@@ -296,11 +315,12 @@ __global__ void __launch_bounds__(kScoreThreads) k_intpoly_score(const IntpolyAr
         const uint64_t nt = a.term_ptr[o0 + 1] - a.term_ptr[o0];
         const uint32_t me = tid >> 8, q4 = tid & 255u;  // group member, point quad
         const bool active = me < gm;
-        // unreduced sums of lazy Montgomery products (each < 2p, so a sum of
-        // fewer than 2^31 terms fits 64 bits), reduced once after the terms
-        uint64_t acc[16];  // [poly * 2 + prime][4]
+        // exact sums of products of centred residues (one widening multiply-add
+        // each), folded every kFoldSteps terms and reduced mod p after the last
+        int64_t acc[16];  // [poly * 2 + prime][4]
 #pragma unroll
         for (int e = 0; e < 16; ++e) acc[e] = 0;
+        uint32_t since_fold = 0;
         // kScoreStepTerms row steps per barrier: the stages they used are
         // refilled together after it
         for (uint64_t i = 0; i < nt; i += kScoreStepTerms) {
@@ -314,15 +334,20 @@ __global__ void __launch_bounds__(kScoreThreads) k_intpoly_score(const IntpolyAr
                     const uint4 *cv = reinterpret_cast<const uint4 *>(st);
                     const uint4 *wv = reinterpret_cast<const uint4 *>(st + (4 + 2 * me) * N);
                     const uint4 w0 = wv[q4], w1 = wv[N / 4 + q4];
-                    const uint32_t W[2][4] = {{w0.x, w0.y, w0.z, w0.w}, {w1.x, w1.y, w1.z, w1.w}};
+                    const int32_t W[2][4] = {{int32_t(w0.x), int32_t(w0.y), int32_t(w0.z), int32_t(w0.w)},
+                                             {int32_t(w1.x), int32_t(w1.y), int32_t(w1.z), int32_t(w1.w)}};
 #pragma unroll
                     for (int ap = 0; ap < 4; ++ap) {  // (poly, prime)
                         const uint4 c = cv[ap * (N / 4) + q4];
-                        const uint32_t Cv[4] = {c.x, c.y, c.z, c.w};
+                        const int32_t Cv[4] = {int32_t(c.x), int32_t(c.y), int32_t(c.z), int32_t(c.w)};
                         const int q = ap & 1;
-                        const uint32_t p = q ? p1 : p0, pinv = q ? i1 : i0;
 #pragma unroll
-                        for (int e = 0; e < 4; ++e) acc[ap * 4 + e] += mont_mul_lazy(W[q][e], Cv[e], p, pinv);
+                        for (int e = 0; e < 4; ++e) acc[ap * 4 + e] = mad_wide(W[q][e], Cv[e], acc[ap * 4 + e]);
+                    }
+                    if (++since_fold == kFoldSteps) {
+                        since_fold = 0;
+#pragma unroll
+                        for (int e = 0; e < 16; ++e) acc[e] = fold(acc[e], (e >> 2) & 1 ? f1 : f0);
                     }
                 }
                 ++consumed;
@@ -334,41 +359,98 @@ __global__ void __launch_bounds__(kScoreThreads) k_intpoly_score(const IntpolyAr
                 for (uint32_t d = 0; d < steps; ++d) issue_next();
         }
         if (!ok) break;
+        // Inverse NTT (Gentleman-Sande; the stage of span t pairs points j and
+        // j + t with twiddle itw[N / (2t) + j / (2t)]), in three parts.
+        // (1) Each sum to its residue times 2^-32 (REDC), then the stages t = 1
+        // and 2, which stay inside this thread's points 4q..4q+3.
         if (active) {
 #pragma unroll
             for (int ap = 0; ap < 4; ++ap) {
                 const int q = ap & 1;
                 const uint32_t p = q ? p1 : p0, pinv = q ? i1 : i0;
+                uint32_t v[4];
 #pragma unroll
                 for (int e = 0; e < 4; ++e) {
-                    // REDC of the 64-bit sum T (< p * 2^32): u = T * 2^-32 mod p,
-                    // then * 2^64 * 2^-32 (Montgomery product with R^2) gives T mod p
-                    const uint64_t T = acc[ap * 4 + e];
+                    // fold below 2^49 and lift by p * 2^19 to a positive T < p * 2^32
+                    const uint64_t T = uint64_t(fold(acc[ap * 4 + e], q ? f1 : f0) + (int64_t(p) << 19));
                     const uint32_t m = uint32_t(T) * pinv;
-                    uint32_t u = uint32_t((T + uint64_t(m) * p) >> 32);
-                    u = u >= p ? u - p : u;
-                    arr[(4 * me + ap) * N + 4 * q4 + e] = mont_mul(u, a.k.r2[q], p, pinv);
+                    const uint32_t u = uint32_t((T + uint64_t(m) * p) >> 32);
+                    v[e] = u >= p ? u - p : u;
                 }
+                const uint32_t *tw = itws + q * N;
+                gs_butterfly(v[0], v[1], tw[N / 2 + 2 * q4], p, pinv);
+                gs_butterfly(v[2], v[3], tw[N / 2 + 2 * q4 + 1], p, pinv);
+                const uint32_t s2 = tw[N / 4 + q4];
+                gs_butterfly(v[0], v[2], s2, p, pinv);
+                gs_butterfly(v[1], v[3], s2, p, pinv);
+                reinterpret_cast<uint4 *>(arr + (4 * me + ap) * N)[q4] = make_uint4(v[0], v[1], v[2], v[3]);
             }
         }
         __syncthreads();
-        ntt_inverse(arr, int(4 * gm), N, itws, a.k, [](uint32_t x) { return x & 1u; });
-        // CRT: x = x1 + p1 * ((x2 - x1) / p1 mod p2), signed, then mod 2^32
-        for (uint32_t x = tid; x < 2 * N * gm; x += blockDim.x) {
-            const uint32_t m = x / (2 * N), pl = (x / N) % 2, j = x % N;
+        // (2) Stages (4, 8), (16, 32), (64, 128) as radix-4 passes: item w of
+        // an array takes points base + r + {0, t, 2t, 3t}, base = 4t * (w / t).
+#pragma unroll 1
+        for (uint32_t lt = 2; lt <= 6; lt += 2) {
+            const uint32_t t = 1u << lt, h = N >> (lt + 1);
+            for (uint32_t x = tid; x < 4 * gm * (N / 4); x += blockDim.x) {
+                const uint32_t ar = x / (N / 4), w = x % (N / 4);
+                const uint32_t kb = w >> lt, r = w & (t - 1);
+                const uint32_t q = ar & 1u;
+                const uint32_t p = q ? p1 : p0, pinv = q ? i1 : i0;
+                uint32_t *va = arr + ar * N + 4 * t * kb + r;
+                const uint32_t *tw = itws + q * N;
+                uint32_t x0 = va[0], x1 = va[t], x2 = va[2 * t], x3 = va[3 * t];
+                gs_butterfly(x0, x1, tw[h + 2 * kb], p, pinv);
+                gs_butterfly(x2, x3, tw[h + 2 * kb + 1], p, pinv);
+                const uint32_t s = tw[h / 2 + kb];
+                gs_butterfly(x0, x2, s, p, pinv);
+                gs_butterfly(x1, x3, s, p, pinv);
+                va[0] = x0;
+                va[t] = x1;
+                va[2 * t] = x2;
+                va[3 * t] = x3;
+            }
+            __syncthreads();
+        }
+        // (3) Stages 256 and 512 in registers, scaled by N^-1 * 2^32 (which
+        // also undoes the REDC factor), then CRT and the epilogue: item
+        // (member, poly, r) finishes points r + 256e of both primes.
+        for (uint32_t x = tid; x < gm * 2 * (N / 4); x += blockDim.x) {
+            const uint32_t m = x / (N / 2), pl = (x / (N / 4)) & 1u, r = x % (N / 4);
             const uint64_t o = o0 + m;
             if (o < a.out_begin || o >= a.out_end) continue;
-            const uint32_t x1 = arr[(4 * m + 2 * pl) * N + j], x2 = arr[(4 * m + 2 * pl + 1) * N + j];
-            const uint32_t x1m = x1 >= p1 ? x1 - p1 : x1;
-            const uint32_t t = mont_mul(mod_sub(x2, x1m, p1), a.k.p1inv_m, p1, i1);
-            uint64_t v = uint64_t(x1) + uint64_t(p0) * t;
-            uint32_t w = uint32_t(v);
-            if (v > a.k.M_half) w -= uint32_t(a.k.M);
-            if (pl == 1) {
-                if (j < a.num_samples) w += uint32_t(a.bias ? a.bias[o] : 0) * uint32_t(a.one);
-                if (j >= a.region_size) w = 0;
+            uint32_t y[2][4];
+#pragma unroll
+            for (int q = 0; q < 2; ++q) {
+                const uint32_t p = q ? p1 : p0, pinv = q ? i1 : i0;
+                const uint32_t *va = arr + (4 * m + 2 * pl + q) * N + r;
+                const uint32_t *tw = itws + q * N;
+                uint32_t x0 = va[0], x1 = va[N / 4], x2 = va[N / 2], x3 = va[3 * N / 4];
+                gs_butterfly(x0, x1, tw[2], p, pinv);
+                gs_butterfly(x2, x3, tw[3], p, pinv);
+                y[q][0] = mont_mul(mod_add(x0, x2, p), a.k.nscale[q], p, pinv);
+                y[q][1] = mont_mul(mod_add(x1, x3, p), a.k.nscale[q], p, pinv);
+                y[q][2] = mont_mul(mod_sub(x0, x2, p), a.k.nscale_tw[q], p, pinv);
+                y[q][3] = mont_mul(mod_sub(x1, x3, p), a.k.nscale_tw[q], p, pinv);
             }
-            reinterpret_cast<uint32_t *>(a.out + (o - a.out_begin) * a.out_stride)[pl * N + j] = w;
+            uint32_t *dst = reinterpret_cast<uint32_t *>(a.out + (o - a.out_begin) * a.out_stride) + pl * N;
+            const uint32_t add = pl == 1 && a.bias ? uint32_t(a.bias[o]) * uint32_t(a.one) : 0u;
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                // CRT: x = x1 + p1 * ((x2 - x1) / p1 mod p2), signed, then mod 2^32
+                const uint32_t j = r + e * (N / 4);
+                const uint32_t x1 = y[0][e], x2 = y[1][e];
+                const uint32_t x1m = x1 >= p1 ? x1 - p1 : x1;
+                const uint32_t t = mont_mul(mod_sub(x2, x1m, p1), a.k.p1inv_m, p1, i1);
+                const uint64_t v = uint64_t(x1) + uint64_t(p0) * t;
+                uint32_t w = uint32_t(v);
+                if (v > a.k.M_half) w -= uint32_t(a.k.M);
+                if (pl == 1) {
+                    if (j < a.num_samples) w += add;
+                    if (j >= a.region_size) w = 0;
+                }
+                dst[j] = w;
+            }
         }
         __syncthreads();  // arr is read before the next group overwrites it
     }
@@ -395,8 +477,12 @@ NttConsts make_consts(uint32_t N) {
         for (int it = 0; it < 5; ++it) inv *= 2u - uint32_t(p) * inv;
         k.pinv[q] = 0u - inv;
         const uint64_t R = (uint64_t(1) << 32) % p;
-        k.r2[q] = uint32_t(mulmod(R, R, p));
-        k.ninv[q] = uint32_t(mulmod(powmod(N, p - 2, p), R, p));
+        k.r1[q] = int32_t(R);
+        const uint64_t nscale = mulmod(powmod(N, p - 2, p), mulmod(R, R, p), p);
+        k.nscale[q] = uint32_t(nscale);
+        // the last inverse stage's twiddle: psi^-(N/2) (bit-reversed index 1)
+        const uint64_t psi = powmod(kPsi2048[q], 2048 / (2 * N), p);
+        k.nscale_tw[q] = uint32_t(mulmod(powmod(powmod(psi, p - 2, p), N / 2, p), nscale, p));
     }
     const uint64_t p0 = kPrimes[0], p1 = kPrimes[1];
     k.p1inv_m = uint32_t(mulmod(powmod(p0 % p1, p1 - 2, p1), (uint64_t(1) << 32) % p1, p1));
@@ -473,7 +559,7 @@ extern "C" idash_status idash_model_intpoly(idash_ctx *ctx, idash_model **model,
                                             int term_poly_on_device) {
     if (!ctx || !model || !p || (n_out && !term_ptr)) return IDASH_ERR_INVALID_ARGUMENT;
     *model = nullptr;
-    if (p->N != 4 * kNttThreads)
+    if (p->N != kIpN)
         return ctx->fail(IDASH_ERR_UNSUPPORTED, "the integer-polynomial kernels are built for N = 1024");
     if (p->num_samples > p->region_size || p->region_size > p->N)
         return ctx->fail(IDASH_ERR_INVALID_ARGUMENT, "need num_samples <= region_size <= N");
