@@ -34,6 +34,7 @@ namespace {
 constexpr uint32_t kPrimes[2] = {2147473409u, 2147389441u};  // both = 1 mod 2048
 constexpr uint32_t kPsi2048[2] = {383167813u, 211808905u};   // primitive 2048-th roots of unity
 constexpr int kNttThreads = 256;
+constexpr uint32_t kIpN = 1024;  // polynomial size of the row and scoring kernels: 256 threads x 4 points
 
 // 2^32 mod p is small for both primes (20478 and 188414), so folding the high
 // word of a 64-bit sum onto the low one with it shrinks the sum below 2^49.
@@ -72,10 +73,22 @@ __device__ __forceinline__ uint32_t mont_mul(uint32_t a, uint32_t b, uint32_t p,
     return r >= p ? r - p : r;
 }
 
-// A signed 32-bit word (or int16) as a residue mod p.
+// A signed 32-bit word (or int16) as a residue mod p, for 2^30 < p < 2^31:
+// v + 2p is positive and below 4p, so at most two corrections either way.
 __device__ __forceinline__ uint32_t residue(int32_t v, uint32_t p) {
-    int64_t x = int64_t(v) % int64_t(p);
-    return uint32_t(x < 0 ? x + p : x);
+    int64_t x = v;
+    x += x < 0 ? int64_t(p) : 0;
+    x += x < 0 ? int64_t(p) : 0;
+    x -= x >= int64_t(p) ? int64_t(p) : 0;
+    return uint32_t(x);
+}
+static_assert(kPrimes[0] > (1u << 30) && kPrimes[1] > (1u << 30), "residue() needs p > 2^30");
+
+// Cooley-Tukey butterfly of the forward transform: (u, v) -> (u + v*S, u - v*S).
+__device__ __forceinline__ void ct_butterfly(uint32_t &u, uint32_t &v, uint32_t S, uint32_t p, uint32_t pinv) {
+    const uint32_t w = mont_mul(v, S, p, pinv);
+    v = mod_sub(u, w, p);
+    u = mod_add(u, w, p);
 }
 
 // A residue x in [0, p) as the congruent value in (-p/2, p/2]: transforms are
@@ -139,34 +152,92 @@ __global__ void __launch_bounds__(kNttThreads) k_ntt_model(const int16_t *w, uin
     }
 }
 
-// Input TRLWE rows (a | b, signed words) -> NTT, centred residues, [row][poly][prime][N].
+// Input TRLWE rows (a | b, signed words) -> NTT, centred residues,
+// [row][poly][prime][N], N = kIpN, kNttThreads threads.  The stage of span t
+// pairs points j and j + t with twiddle tw[N / (2t) + j / (2t)].  Per row:
+// (1) thread r loads points r + 256e of both polynomials and does the stages
+// 512 and 256 in registers, for both primes; (2) stages (128, 64), (32, 16),
+// (8, 4) as radix-4 passes in shared memory; (3) stages 2 and 1 in registers
+// on 4 consecutive points, stored straight to global memory.  Two shared
+// buffers alternate between rows.
 __global__ void __launch_bounds__(kNttThreads) k_ntt_rows(const uint8_t *in, uint64_t stride, uint64_t n_rows,
-                                                          uint32_t N, const uint32_t *tw, NttConsts k,
-                                                          uint32_t *c_hat) {
+                                                          const uint32_t *tw, NttConsts k, uint32_t *c_hat) {
+    constexpr uint32_t N = kIpN, Q = N / 4;
     extern __shared__ uint32_t sh[];
-    uint32_t *tws = sh;          // 2 * N
-    uint32_t *arr = sh + 2 * N;  // 4 arrays: (a,p1) (a,p2) (b,p1) (b,p2)
+    uint32_t *tws = sh;  // 2 * N
     for (uint32_t x = threadIdx.x; x < 2 * N; x += blockDim.x) tws[x] = tw[x];
     __syncthreads();
-    for (uint64_t r = blockIdx.x; r < n_rows; r += gridDim.x) {
-        const int32_t *src = reinterpret_cast<const int32_t *>(in + r * stride);
-        for (uint32_t x = threadIdx.x; x < 2 * N; x += blockDim.x) {
-            const uint32_t poly = x / N, j = x % N;
-            const int32_t v = src[x];
-            arr[(2 * poly) * N + j] = residue(v, k.p[0]);
-            arr[(2 * poly + 1) * N + j] = residue(v, k.p[1]);
+    const uint32_t tid = threadIdx.x;
+    uint32_t buf = 0;
+    for (uint64_t row = blockIdx.x; row < n_rows; row += gridDim.x, buf ^= 1u) {
+        uint32_t *arr = sh + 2 * N + buf * 4 * N;  // 4 arrays: (a,p1) (a,p2) (b,p1) (b,p2)
+        const int32_t *src = reinterpret_cast<const int32_t *>(in + row * stride);
+        // (1)
+#pragma unroll
+        for (uint32_t poly = 0; poly < 2; ++poly) {
+            int32_t v[4];
+#pragma unroll
+            for (int e = 0; e < 4; ++e) v[e] = src[poly * N + tid + e * Q];
+#pragma unroll
+            for (uint32_t q = 0; q < 2; ++q) {
+                const uint32_t p = k.p[q], pinv = k.pinv[q];
+                uint32_t x0 = residue(v[0], p), x1 = residue(v[1], p), x2 = residue(v[2], p), x3 = residue(v[3], p);
+                const uint32_t *t = tws + q * N;
+                ct_butterfly(x0, x2, t[1], p, pinv);
+                ct_butterfly(x1, x3, t[1], p, pinv);
+                ct_butterfly(x0, x1, t[2], p, pinv);
+                ct_butterfly(x2, x3, t[3], p, pinv);
+                uint32_t *a = arr + (2 * poly + q) * N + tid;
+                a[0] = x0;
+                a[Q] = x1;
+                a[2 * Q] = x2;
+                a[3 * Q] = x3;
+            }
         }
         __syncthreads();
-        ntt_forward(arr, 4, uint32_t(__ffs(N) - 1), tws, k, [](uint32_t a) { return a & 1u; });
-        uint4 *dst = reinterpret_cast<uint4 *>(c_hat + r * 4 * N);
-        const uint4 *s4 = reinterpret_cast<const uint4 *>(arr);
-        for (uint32_t x = threadIdx.x; x < N; x += blockDim.x) {
-            const uint32_t p = k.p[(4 * x / N) & 1u];  // 4 words of one (poly, prime) array
-            const uint4 v = s4[x];
-            dst[x] = make_uint4(uint32_t(centred(v.x, p)), uint32_t(centred(v.y, p)), uint32_t(centred(v.z, p)),
-                                uint32_t(centred(v.w, p)));
+        // (2) item w: points base + r + {0, T/2, T, 3T/2}, base = 2T * (w / (T/2))
+#pragma unroll 1
+        for (uint32_t lt = 7; lt >= 3; lt -= 2) {  // T = 2^lt
+            const uint32_t T = 1u << lt, h = T / 2, m = N >> (lt + 1);
+            for (uint32_t x = tid; x < 4 * Q; x += blockDim.x) {
+                const uint32_t ar = x / Q, w = x % Q;
+                const uint32_t kb = w >> (lt - 1), r = w & (h - 1);
+                const uint32_t q = ar & 1u;
+                const uint32_t p = k.p[q], pinv = k.pinv[q];
+                const uint32_t *t = tws + q * N;
+                uint32_t *va = arr + ar * N + 2 * T * kb + r;
+                uint32_t x0 = va[0], x1 = va[h], x2 = va[T], x3 = va[T + h];
+                const uint32_t s = t[m + kb];
+                ct_butterfly(x0, x2, s, p, pinv);
+                ct_butterfly(x1, x3, s, p, pinv);
+                ct_butterfly(x0, x1, t[2 * m + 2 * kb], p, pinv);
+                ct_butterfly(x2, x3, t[2 * m + 2 * kb + 1], p, pinv);
+                va[0] = x0;
+                va[h] = x1;
+                va[T] = x2;
+                va[T + h] = x3;
+            }
+            __syncthreads();
         }
-        __syncthreads();
+        // (3) points 4w..4w+3: stage 2 (twiddle N/4 + w), stage 1 (N/2 + 2w, N/2 + 2w + 1)
+        uint4 *dst = reinterpret_cast<uint4 *>(c_hat + row * 4 * N);
+        for (uint32_t x = tid; x < 4 * Q; x += blockDim.x) {
+            const uint32_t ar = x / Q, w = x % Q;
+            const uint32_t q = ar & 1u;
+            const uint32_t p = k.p[q], pinv = k.pinv[q];
+            const uint32_t *t = tws + q * N;
+            const uint4 v = reinterpret_cast<const uint4 *>(arr)[x];
+            uint32_t x0 = v.x, x1 = v.y, x2 = v.z, x3 = v.w;
+            const uint32_t s = t[N / 4 + w];
+            ct_butterfly(x0, x2, s, p, pinv);
+            ct_butterfly(x1, x3, s, p, pinv);
+            ct_butterfly(x0, x1, t[N / 2 + 2 * w], p, pinv);
+            ct_butterfly(x2, x3, t[N / 2 + 2 * w + 1], p, pinv);
+            dst[x] = make_uint4(uint32_t(centred(x0, p)), uint32_t(centred(x1, p)), uint32_t(centred(x2, p)),
+                                uint32_t(centred(x3, p)));
+        }
+        // the other buffer is free: its last reader finished before the
+        // barriers of this row
     }
 }
 
@@ -188,7 +259,6 @@ struct IntpolyArgs {
     uint32_t *err;
 };
 
-constexpr uint32_t kIpN = 1024;      // polynomial size of the scoring kernel: 256 threads x 4 points
 constexpr uint32_t kGroupMax = 3;     // outputs sharing one term-row list (a target's genotypes)
 constexpr int kScoreThreads = 256 * kGroupMax;  // k_intpoly_score: 256 threads per group member
 constexpr uint32_t kScoreStages = 4;     // row steps in flight per CTA
@@ -688,12 +758,15 @@ extern "C" idash_status idash_score_intpoly_device(idash_model *m, const void *d
             return s;
         ip.c_hat_rows = ip.n_rows;
     }
-    const size_t smem_rows = size_t(6) * ip.N * 4;
-    const uint32_t grid_rows = uint32_t(std::min<uint64_t>(ip.n_rows, uint64_t(ctx->sm_count) * 8));
+    const size_t smem_rows = size_t(10) * kIpN * 4;  // twiddles and two row buffers
+    int rows_per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&rows_per_sm, k_ntt_rows, kNttThreads, smem_rows) != cudaSuccess ||
+        rows_per_sm < 1)
+        rows_per_sm = 1;
+    const uint32_t grid_rows = uint32_t(std::min<uint64_t>(ip.n_rows, uint64_t(ctx->sm_count) * rows_per_sm));
     if (grid_rows) {
         k_ntt_rows<<<grid_rows, kNttThreads, smem_rows, st>>>(static_cast<const uint8_t *>(d_in) + il->payload_offset,
-                                                             il->row_stride, ip.n_rows, ip.N, ip.d_tw, ip.k,
-                                                             ip.d_c_hat);
+                                                             il->row_stride, ip.n_rows, ip.d_tw, ip.k, ip.d_c_hat);
         if ((s = ctx->check_cuda(cudaGetLastError(), "k_ntt_rows launch")) != IDASH_OK) return s;
     }
     IntpolyArgs a{};
