@@ -260,9 +260,9 @@ struct IntpolyArgs {
 };
 
 constexpr uint32_t kGroupMax = 3;     // outputs sharing one term-row list (a target's genotypes)
-constexpr int kScoreThreads = 256 * kGroupMax;  // k_intpoly_score: 256 threads per group member
-constexpr uint32_t kScoreStages = 4;     // row steps in flight per CTA
-constexpr uint32_t kScoreStepTerms = 1;  // row steps consumed per CTA barrier (2 measured slower)
+constexpr int kScoreThreads = 256 * kGroupMax;  // k_intpoly_score consumers: 256 threads per group member
+constexpr int kScoreBlock = kScoreThreads + 32;  // and one producer warp
+constexpr uint32_t kScoreStages = 4;             // row steps in flight per CTA
 // Products of centred residues have magnitude below 2^60; a folded sum is
 // below 2^49, so kFoldSteps products more stay below 2^63.
 constexpr uint32_t kFoldSteps = 7;
@@ -287,11 +287,6 @@ __device__ __forceinline__ int64_t fold(int64_t T, int32_t r1) {
     return d;
 }
 
-__device__ __forceinline__ void ip_mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
-                 : "memory");
-}
-
 // Stage layout: the input row's transform (2 polynomials x 2 primes x N
 // words), then the weight transforms (2 primes x N words) of up to kGroupMax
 // outputs at the same term position.
@@ -300,90 +295,127 @@ __host__ __device__ constexpr size_t ip_score_smem(uint32_t N) {
     return 128 + (size_t(kScoreStages) * ip_stage_words(N) + 4 * size_t(kGroupMax) * N + 2 * size_t(N)) * 4;
 }
 
+// Consumer-only synchronisation (named barrier 1): the producer warp takes
+// no part in the pointwise phase or the inverse NTT.
+__device__ __forceinline__ void consumers_sync() {
+    asm volatile("bar.sync 1, %0;" ::"n"(kScoreThreads) : "memory");
+}
+__device__ __forceinline__ bool consumers_and(bool v) {
+    uint32_t r;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\t"
+        "setp.ne.u32 p, %1, 0;\n\t"
+        "bar.red.and.pred q, 1, %2, p;\n\t"
+        "selp.u32 %0, 1, 0, q;\n\t}"
+        : "=r"(r)
+        : "r"(v ? 1u : 0u), "n"(kScoreThreads)
+        : "memory");
+    return r != 0;
+}
+
 // One CTA per output group (grid-stride): the outputs of a group read the
 // same input rows in the same order (normally the three genotype outputs of a
 // target), so each row step brings one input transform (16 KiB) and one
-// weight transform (8 KiB) per output.  Thread 0 keeps kScoreStages row steps
-// in flight with cp.async.bulk into a ring completed on mbarriers, across
-// group boundaries; the CTA computes on the oldest stage (thread x: group
-// member x / 256, NTT points 4q..4q+3 of its four arrays, q = x % 256),
-// agrees at a barrier that it is free, and thread 0 refills it.  A product
-// is one signed widening multiply-add into a 64-bit sum; every kFoldSteps
-// terms the sums are folded with 2^32 mod p, which keeps them exact without
-// a Montgomery reduction per product.  Then inverse NTTs, CRT and the a1
-// epilogue per output.  Every wait is bounded; a CTA whose copy never lands
-// drains its copies in flight and stops.
-__global__ void __launch_bounds__(kScoreThreads) k_intpoly_score(const IntpolyArgs a) {
+// weight transform (8 KiB) per output.  A producer warp (one lane) keeps
+// kScoreStages row steps in flight with cp.async.bulk into a ring: stage s
+// completes on full[s], and is refilled once every consumer warp has arrived
+// on empty[s], across group boundaries.  Consumer thread x takes group member
+// x / 256 and NTT points 4q..4q+3 of its four arrays (q = x % 256); warps run
+// through the row steps without a CTA-wide barrier.  A product is one signed
+// widening multiply-add into a 64-bit sum; every kFoldSteps terms the sums
+// are folded with 2^32 mod p, which keeps them exact without a Montgomery
+// reduction per product.  The consumers agree once per group that every copy
+// landed, then run the inverse NTTs, CRT and the a1 epilogue.  Every wait is
+// bounded; after a failed wait the consumers stop together at the group's
+// agreement, and the producer drains its copies in flight before it returns.
+__global__ void __launch_bounds__(kScoreBlock, 1) k_intpoly_score(const IntpolyArgs a) {
     extern __shared__ __align__(128) uint8_t ip_smem[];
     constexpr uint32_t N = kIpN;  // a.N, checked on the host
     uint64_t *full = reinterpret_cast<uint64_t *>(ip_smem);             // [kScoreStages]
+    uint64_t *empty = full + kScoreStages;                              // [kScoreStages]
     uint32_t *stage0 = reinterpret_cast<uint32_t *>(ip_smem + 128);     // kScoreStages x stage
     uint32_t *arr = stage0 + kScoreStages * ip_stage_words(N);          // [output][poly][prime][N]
     uint32_t *itws = arr + 4 * kGroupMax * N;                           // 2N inverse twiddles
     const uint32_t tid = threadIdx.x;
     if (tid == 0) {
-        for (uint32_t s = 0; s < kScoreStages; ++s) mbar_init(&full[s], 1);
+        for (uint32_t s = 0; s < kScoreStages; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], kScoreThreads / 32);
+        }
         fence_mbar_init();
     }
     for (uint32_t x = tid; x < 2 * N; x += blockDim.x) itws[x] = a.itw[x];
     __syncthreads();
 
-    // Fetch cursor (thread 0): the next (group, row step) of this CTA, with
-    // the row of that step loaded one issue ahead.
-    uint64_t f_g = a.group_begin + blockIdx.x, f_i = 0, f_n = 0;
-    uint64_t f_w[kGroupMax] = {0, 0, 0};  // weight index of the group's first term, per member
-    uint32_t f_m = 0;                     // members of the group
-    uint32_t pre_r = 0;
-    uint64_t issued = 0;
-    auto open_group = [&]() {
-        const uint64_t o0 = a.group_first[f_g];
-        f_m = uint32_t(a.group_first[f_g + 1] - o0);
+    if (tid >= kScoreThreads) {
+        // ------------------------------------------------------------ producer
+        if (tid != kScoreThreads) return;
+        // Fetch cursor: the next (group, row step) of this CTA, with the row
+        // of that step loaded one issue ahead.
+        uint64_t f_g = a.group_begin + blockIdx.x, f_i = 0, f_n = 0;
+        uint64_t f_w[kGroupMax] = {0, 0, 0};  // weight index of the group's first term, per member
+        uint32_t f_m = 0;                     // members of the group
+        uint32_t pre_r = 0;
+        auto open_group = [&]() {
+            const uint64_t o0 = a.group_first[f_g];
+            f_m = uint32_t(a.group_first[f_g + 1] - o0);
 #pragma unroll
-        for (uint32_t m = 0; m < kGroupMax; ++m) f_w[m] = m < f_m ? a.term_ptr[o0 + m] : 0;
-        f_i = 0;
-        f_n = a.term_ptr[o0 + 1] - f_w[0];
-    };
-    auto advance = [&]() {
-        while (f_g < a.group_end && f_i >= f_n) {  // skip finished and empty groups
-            f_g += gridDim.x;
-            if (f_g < a.group_end) open_group();
-        }
-        if (f_g < a.group_end) pre_r = a.term_row[f_w[0] + f_i];
-    };
-    auto issue_next = [&]() {
+            for (uint32_t m = 0; m < kGroupMax; ++m) f_w[m] = m < f_m ? a.term_ptr[o0 + m] : 0;
+            f_i = 0;
+            f_n = a.term_ptr[o0 + 1] - f_w[0];
+        };
+        auto advance = [&]() {
+            while (f_g < a.group_end && f_i >= f_n) {  // skip finished and empty groups
+                f_g += gridDim.x;
+                if (f_g < a.group_end) open_group();
+            }
+            if (f_g < a.group_end) pre_r = a.term_row[f_w[0] + f_i];
+        };
         if (f_g >= a.group_end) return;
-        uint32_t r = pre_r;
-        if (r >= a.n_rows) {
-            report_error(a.err, kDevBadIndex);
-            r = 0;  // read a valid row; the output is reported invalid
-        }
-        const uint32_t s = uint32_t(issued % kScoreStages);
-        uint32_t *st = stage0 + s * ip_stage_words(N);
-        fence_proxy_async_smem();
-        ip_mbar_expect_tx(&full[s], (4 + 2 * f_m) * N * 4);
-        bulk_g2s(st, a.c_hat + uint64_t(r) * 4 * N, 4 * N * 4, &full[s]);
-#pragma unroll
-        for (uint32_t m = 0; m < kGroupMax; ++m)
-            if (m < f_m) bulk_g2s(st + (4 + 2 * m) * N, a.w_hat + (f_w[m] + f_i) * 2 * N, 2 * N * 4, &full[s]);
-        ++issued;
-        ++f_i;
-        advance();
-    };
-    if (tid == 0 && f_g < a.group_end) {
         open_group();
         advance();
-        for (uint32_t i = 0; i < kScoreStages; ++i) issue_next();
+        uint64_t issued = 0;
+        bool ok = true;
+        while (f_g < a.group_end) {
+            const uint32_t s = uint32_t(issued % kScoreStages);
+            if (issued >= kScoreStages &&
+                !mbar_wait_bounded(&empty[s], uint32_t((issued / kScoreStages - 1) & 1u), a.err)) {
+                ok = false;
+                break;
+            }
+            uint32_t r = pre_r;
+            if (r >= a.n_rows) {
+                report_error(a.err, kDevBadIndex);
+                r = 0;  // read a valid row; the output is reported invalid
+            }
+            uint32_t *st = stage0 + s * ip_stage_words(N);
+            fence_proxy_async_smem();
+            mbar_arrive_expect_tx(&full[s], (4 + 2 * f_m) * N * 4);
+            bulk_g2s(st, a.c_hat + uint64_t(r) * 4 * N, 4 * N * 4, &full[s]);
+#pragma unroll
+            for (uint32_t m = 0; m < kGroupMax; ++m)
+                if (m < f_m) bulk_g2s(st + (4 + 2 * m) * N, a.w_hat + (f_w[m] + f_i) * 2 * N, 2 * N * 4, &full[s]);
+            ++issued;
+            ++f_i;
+            advance();
+        }
+        if (!ok) {
+            // the consumers stopped: let the copies still in flight land
+            for (uint64_t k = issued > kScoreStages ? issued - kScoreStages : 0; k < issued; ++k)
+                mbar_wait_bounded(&full[k % kScoreStages], uint32_t((k / kScoreStages) & 1u), nullptr);
+        }
+        return;
     }
 
+    // --------------------------------------------------------------- consumers
     const uint32_t p0 = a.k.p[0], p1 = a.k.p[1], i0 = a.k.pinv[0], i1 = a.k.pinv[1];
     const int32_t f0 = a.k.r1[0], f1 = a.k.r1[1];
+    const uint32_t me = tid >> 8, q4 = tid & 255u;  // group member, point quad
     uint64_t consumed = 0;
-    bool ok = true;
-    for (uint64_t g = a.group_begin + blockIdx.x; g < a.group_end && ok; g += gridDim.x) {
+    for (uint64_t g = a.group_begin + blockIdx.x; g < a.group_end; g += gridDim.x) {
         const uint64_t o0 = a.group_first[g];
         const uint32_t gm = uint32_t(a.group_first[g + 1] - o0);
         const uint64_t nt = a.term_ptr[o0 + 1] - a.term_ptr[o0];
-        const uint32_t me = tid >> 8, q4 = tid & 255u;  // group member, point quad
         const bool active = me < gm;
         // exact sums of products of centred residues (one widening multiply-add
         // each), folded every kFoldSteps terms and reduced mod p after the last
@@ -391,44 +423,38 @@ __global__ void __launch_bounds__(kScoreThreads) k_intpoly_score(const IntpolyAr
 #pragma unroll
         for (int e = 0; e < 16; ++e) acc[e] = 0;
         uint32_t since_fold = 0;
-        // kScoreStepTerms row steps per barrier: the stages they used are
-        // refilled together after it
-        for (uint64_t i = 0; i < nt; i += kScoreStepTerms) {
-            const uint32_t steps = nt - i < kScoreStepTerms ? uint32_t(nt - i) : kScoreStepTerms;
-            bool got = true;
-            for (uint32_t d = 0; d < steps; ++d) {
-                const uint32_t s = uint32_t(consumed % kScoreStages);
-                got = mbar_wait_bounded(&full[s], uint32_t((consumed / kScoreStages) & 1u), a.err) && got;
-                if (active) {
-                    const uint32_t *st = stage0 + s * ip_stage_words(N);
-                    const uint4 *cv = reinterpret_cast<const uint4 *>(st);
-                    const uint4 *wv = reinterpret_cast<const uint4 *>(st + (4 + 2 * me) * N);
-                    const uint4 w0 = wv[q4], w1 = wv[N / 4 + q4];
-                    const int32_t W[2][4] = {{int32_t(w0.x), int32_t(w0.y), int32_t(w0.z), int32_t(w0.w)},
-                                             {int32_t(w1.x), int32_t(w1.y), int32_t(w1.z), int32_t(w1.w)}};
+        bool got = true;  // every copy of this group's steps landed
+        for (uint64_t i = 0; i < nt && got; ++i) {
+            const uint32_t s = uint32_t(consumed % kScoreStages);
+            got = mbar_wait_bounded(&full[s], uint32_t((consumed / kScoreStages) & 1u), a.err);
+            if (!got) break;  // the stage is not released: its copy may still land
+            if (active) {
+                const uint32_t *st = stage0 + s * ip_stage_words(N);
+                const uint4 *cv = reinterpret_cast<const uint4 *>(st);
+                const uint4 *wv = reinterpret_cast<const uint4 *>(st + (4 + 2 * me) * N);
+                const uint4 w0 = wv[q4], w1 = wv[N / 4 + q4];
+                const int32_t W[2][4] = {{int32_t(w0.x), int32_t(w0.y), int32_t(w0.z), int32_t(w0.w)},
+                                         {int32_t(w1.x), int32_t(w1.y), int32_t(w1.z), int32_t(w1.w)}};
 #pragma unroll
-                    for (int ap = 0; ap < 4; ++ap) {  // (poly, prime)
-                        const uint4 c = cv[ap * (N / 4) + q4];
-                        const int32_t Cv[4] = {int32_t(c.x), int32_t(c.y), int32_t(c.z), int32_t(c.w)};
-                        const int q = ap & 1;
+                for (int ap = 0; ap < 4; ++ap) {  // (poly, prime)
+                    const uint4 c = cv[ap * (N / 4) + q4];
+                    const int32_t Cv[4] = {int32_t(c.x), int32_t(c.y), int32_t(c.z), int32_t(c.w)};
+                    const int q = ap & 1;
 #pragma unroll
-                        for (int e = 0; e < 4; ++e) acc[ap * 4 + e] = mad_wide(W[q][e], Cv[e], acc[ap * 4 + e]);
-                    }
-                    if (++since_fold == kFoldSteps) {
-                        since_fold = 0;
-#pragma unroll
-                        for (int e = 0; e < 16; ++e) acc[e] = fold(acc[e], (e >> 2) & 1 ? f1 : f0);
-                    }
+                    for (int e = 0; e < 4; ++e) acc[ap * 4 + e] = mad_wide(W[q][e], Cv[e], acc[ap * 4 + e]);
                 }
-                ++consumed;
+                if (++since_fold == kFoldSteps) {
+                    since_fold = 0;
+#pragma unroll
+                    for (int e = 0; e < 16; ++e) acc[e] = fold(acc[e], (e >> 2) & 1 ? f1 : f0);
+                }
             }
-            // every thread is done with these stages (and agrees the copies landed)
-            ok = __syncthreads_and(got ? 1 : 0) != 0;
-            if (!ok) break;
-            if (tid == 0)
-                for (uint32_t d = 0; d < steps; ++d) issue_next();
+            ++consumed;
+            // this warp is done with the stage
+            __syncwarp();
+            if ((tid & 31u) == 0) mbar_arrive(&empty[s]);
         }
-        if (!ok) break;
+        if (!consumers_and(got)) return;  // a copy never landed: all consumers stop here
         // Inverse NTT (Gentleman-Sande; the stage of span t pairs points j and
         // j + t with twiddle itw[N / (2t) + j / (2t)]), in three parts.
         // (1) Each sum to its residue times 2^-32 (REDC), then the stages t = 1
@@ -456,13 +482,13 @@ __global__ void __launch_bounds__(kScoreThreads) k_intpoly_score(const IntpolyAr
                 reinterpret_cast<uint4 *>(arr + (4 * me + ap) * N)[q4] = make_uint4(v[0], v[1], v[2], v[3]);
             }
         }
-        __syncthreads();
+        consumers_sync();
         // (2) Stages (4, 8), (16, 32), (64, 128) as radix-4 passes: item w of
         // an array takes points base + r + {0, t, 2t, 3t}, base = 4t * (w / t).
 #pragma unroll 1
         for (uint32_t lt = 2; lt <= 6; lt += 2) {
             const uint32_t t = 1u << lt, h = N >> (lt + 1);
-            for (uint32_t x = tid; x < 4 * gm * (N / 4); x += blockDim.x) {
+            for (uint32_t x = tid; x < 4 * gm * (N / 4); x += kScoreThreads) {
                 const uint32_t ar = x / (N / 4), w = x % (N / 4);
                 const uint32_t kb = w >> lt, r = w & (t - 1);
                 const uint32_t q = ar & 1u;
@@ -480,12 +506,12 @@ __global__ void __launch_bounds__(kScoreThreads) k_intpoly_score(const IntpolyAr
                 va[2 * t] = x2;
                 va[3 * t] = x3;
             }
-            __syncthreads();
+            consumers_sync();
         }
         // (3) Stages 256 and 512 in registers, scaled by N^-1 * 2^32 (which
         // also undoes the REDC factor), then CRT and the epilogue: item
         // (member, poly, r) finishes points r + 256e of both primes.
-        for (uint32_t x = tid; x < gm * 2 * (N / 4); x += blockDim.x) {
+        for (uint32_t x = tid; x < gm * 2 * (N / 4); x += kScoreThreads) {
             const uint32_t m = x / (N / 2), pl = (x / (N / 4)) & 1u, r = x % (N / 4);
             const uint64_t o = o0 + m;
             if (o < a.out_begin || o >= a.out_end) continue;
@@ -522,12 +548,7 @@ __global__ void __launch_bounds__(kScoreThreads) k_intpoly_score(const IntpolyAr
                 dst[j] = w;
             }
         }
-        __syncthreads();  // arr is read before the next group overwrites it
-    }
-    if (!ok && tid == 0) {
-        // a copy never landed: let every copy still in flight land before exiting
-        for (uint64_t k = consumed > kScoreStepTerms ? consumed - kScoreStepTerms : 0; k < issued; ++k)
-            mbar_wait_bounded(&full[k % kScoreStages], uint32_t((k / kScoreStages) & 1u), nullptr);
+        consumers_sync();  // arr is read before the next group overwrites it
     }
 }
 
@@ -802,12 +823,12 @@ extern "C" idash_status idash_score_intpoly_device(idash_model *m, const void *d
         return s;
     // one wave of resident CTAs, each striding over the groups
     int resident = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, k_intpoly_score, kScoreThreads, smem) != cudaSuccess ||
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, k_intpoly_score, kScoreBlock, smem) != cudaSuccess ||
         resident < 1)
         resident = 1;
     const uint32_t grid = uint32_t(
         std::min<uint64_t>(a.group_end - a.group_begin, uint64_t(ctx->sm_count) * uint64_t(resident)));
-    k_intpoly_score<<<grid, kScoreThreads, smem, st>>>(a);
+    k_intpoly_score<<<grid, kScoreBlock, smem, st>>>(a);
     s = ctx->check_cuda(cudaGetLastError(), "k_intpoly_score launch");
     if (s == IDASH_OK) ctx->stats.kernel_launches += 2;
     return s;

@@ -32,10 +32,6 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
                  : "memory");
 }
 
-__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
-    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
-}
-
 // Epilogue masks over the thread's 4Q columns (bit 4k+e: quad k, element e):
 // which columns receive the bias, which are zeroed.
 template <int Q, int TEAM>
