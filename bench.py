@@ -280,8 +280,9 @@ def section_decrypt(ctx, model, spec, d_out, seed, steps):
     return {"value": model.n_out * ns / (ms / 1e3), "unit": "decrypted scores/s", "ms_per_step": ms,
             "rows": model.n_out, "samples": ns, "key_weight": nz,
             "word_adds_per_s": adds / (ms / 1e3),
-            "kernel": "k_decrypt_phase: one CTA per row, negacyclic extension of the mask in shared memory, "
-                      "4 coefficients per thread (256 apart) over the key's nonzero positions"}
+            "kernel": "k_decrypt_binary: 4 rows per CTA, negacyclic extension of each mask in (bank-padded) "
+                      "shared memory, 16 consecutive coefficients per thread, the key in 32-position chunks: a "
+                      "48-word window in registers per chunk, one uniform branch per key bit"}
 
 
 def section_encrypt(ctx, spec, seed, steps):
