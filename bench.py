@@ -312,8 +312,8 @@ def section_encrypt(ctx, spec, seed, steps):
         b.free()
     return {"value": n_rows / (ms / 1e3), "unit": "TRLWE encryptions/s", "ms_per_step": ms, "rows": n_rows,
             "samples": ns, "key_weight": int(key.sum()),
-            "kernel": "k_encrypt_rows: one CTA per row, counter-based mask and Box-Muller noise, mask*key over "
-                      "the key's nonzero positions, one-hot messages, record headers"}
+            "kernel": "k_encrypt_binary: 4 rows per CTA, counter-based mask and Box-Muller noise, mask*key as a "
+                      "register-windowed product (16 coefficients per thread), one-hot messages, record headers"}
 
 
 def section_lwe(ctx, name, seed, n_indiv, n_tags, n_targets, neighbours=5, choices=None, passes=2, chunk=2048):

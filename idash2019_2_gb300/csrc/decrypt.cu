@@ -13,6 +13,7 @@
 
 #include "capi_internal.hpp"
 #include "common.cuh"
+#include "negacyclic.cuh"
 
 namespace idash {
 namespace {
@@ -74,78 +75,40 @@ __global__ void __launch_bounds__(kDecryptThreads) k_decrypt_phase(const uint8_t
     }
 }
 
-// Binary keys, N a multiple of 32: thread x of a row owns the 16 consecutive
-// coefficients j0 = 16x .. 16x+15 and walks the key in chunks of 32
-// positions.  For chunk c the terms ext[N + j - i] (j in j0..j0+15, i in
-// 32c..32c+31) lie in the 48 words from N + j0 - 32c - 32 (a multiple of 16,
-// so twelve 16-byte loads); each word then serves up to 16 coefficients from
-// registers.  The key's bits are the same for every thread, so each bit test
-// is a uniform branch.  kRowsPerCta rows share a CTA, each with its own ext.
-// Measured on the 242,646 x 1,000 decryption: 8 columns per thread 8.4 ms,
-// 16 columns 7.0 ms, 32 columns 8.1 ms; testing the bits in pairs (one
-// three-input add for two set bits) was slower at every width.
-constexpr uint32_t kBinCols = 16;
-// ext word i is stored at i + 4 * (i / 32): neighbouring threads' windows
-// (kBinCols words apart) then start in different banks
-__host__ __device__ constexpr uint32_t padded(uint32_t i) { return i + ((i >> 5) << 2); }
-
+// Binary keys, N a multiple of 32: the register-windowed product of
+// negacyclic.cuh, kNegCols consecutive coefficients per thread, kRowsPerCta
+// rows per CTA, each with its own padded extension.  Measured on the
+// 242,646 x 1,000 decryption: 8 columns per thread 8.4 ms, 16 columns 7.0 ms,
+// 32 columns 8.1 ms (k_decrypt_phase: 15.2 ms); testing the key bits in
+// pairs (one three-input add for two set bits) was slower at every width.
 template <uint32_t kRowThreads>
 __global__ void __launch_bounds__(kDecryptThreads) k_decrypt_binary(const uint8_t *in, uint64_t in_stride, uint32_t N,
                                                                     uint32_t num_samples, const uint32_t *key_idx,
                                                                     uint32_t n_nz, uint64_t n_rows, float *out) {
     constexpr uint32_t kRowsPerCta = kDecryptThreads / kRowThreads;
     extern __shared__ __align__(16) uint32_t sh[];
-    uint32_t *mask = sh;                   // N / 32 key words
-    uint32_t *ext_all = sh + (N / 32 + 3) / 4 * 4;  // kRowsPerCta x padded(2N)
-    for (uint32_t w = threadIdx.x; w < N / 32; w += blockDim.x) mask[w] = 0;
-    __syncthreads();
-    for (uint32_t q = threadIdx.x; q < n_nz; q += blockDim.x) atomicOr(&mask[key_idx[q] / 32], 1u << (key_idx[q] % 32));
+    uint32_t *key_mask = sh;
+    uint32_t *ext_all = sh + neg_mask_words(N);  // kRowsPerCta padded extensions
+    neg_build_mask(key_mask, N, key_idx, n_nz);
     const uint32_t sub = threadIdx.x / kRowThreads, x = threadIdx.x % kRowThreads;
-    const uint32_t j0 = kBinCols * x;
-    const uint32_t ext_words = padded(2 * N);
-    uint32_t *ext = ext_all + sub * ext_words;
+    const uint32_t j0 = kNegCols * x;
+    const uint32_t ext_words = neg_ext_words(N);
     for (uint64_t row0 = uint64_t(blockIdx.x) * kRowsPerCta; row0 < n_rows; row0 += uint64_t(gridDim.x) * kRowsPerCta) {
         __syncthreads();  // the previous rows are done with ext (and the key mask is complete)
         for (uint32_t t = threadIdx.x; t < kRowsPerCta * N; t += blockDim.x) {
             const uint32_t s = t / N, k = t % N;
             if (row0 + s >= n_rows) break;
-            const uint32_t v = reinterpret_cast<const uint32_t *>(in + (row0 + s) * in_stride)[k];
-            ext_all[s * ext_words + padded(N + k)] = v;
-            ext_all[s * ext_words + padded(k)] = 0u - v;
+            neg_store(ext_all + s * ext_words, N, k, reinterpret_cast<const uint32_t *>(in + (row0 + s) * in_stride)[k]);
         }
         __syncthreads();
         const uint64_t row = row0 + sub;
         if (row >= n_rows || j0 >= num_samples) continue;
-        uint32_t acc[kBinCols];
-#pragma unroll
-        for (uint32_t r = 0; r < kBinCols; ++r) acc[r] = 0;
-        for (uint32_t c = 0; c < N / 32; ++c) {
-            const uint32_t m = mask[c];
-            if (m == 0) continue;
-            // volatile 16-byte loads: the window stays in registers (the
-            // compiler may not re-issue them inside the bit tests)
-            const uint32_t w0 = N + j0 - 32 * c - 32, wp = smem_addr(ext);
-            uint32_t win[32 + kBinCols];
-#pragma unroll
-            for (uint32_t k = 0; k < (32 + kBinCols) / 4; ++k) {
-                const uint4 v = lds_v4(wp + 4 * padded(w0 + 4 * k));
-                win[4 * k] = v.x;
-                win[4 * k + 1] = v.y;
-                win[4 * k + 2] = v.z;
-                win[4 * k + 3] = v.w;
-            }
-            // key position 32c + p contributes win[32 + r - p] to coefficient j0 + r
-#pragma unroll
-            for (uint32_t p = 0; p < 32; ++p)
-                if (m & (1u << p)) {
-#pragma unroll
-                    for (uint32_t r = 0; r < kBinCols; ++r) acc[r] += win[32 + r - p];
-                }
-        }
+        uint32_t acc[kNegCols];
+        neg_product(ext_all + sub * ext_words, N, j0, key_mask, acc);
         const uint32_t *b = reinterpret_cast<const uint32_t *>(in + row * in_stride) + N;
         float *o = out + row * num_samples;
 #pragma unroll
-        for (uint32_t r = 0; r < kBinCols; ++r) {
+        for (uint32_t r = 0; r < kNegCols; ++r) {
             const uint32_t j = j0 + r;
             if (j < num_samples) o[j] = __int2float_rn(int32_t(b[j] - acc[r])) * 0x1p-32f;
         }
@@ -173,11 +136,11 @@ extern "C" idash_status idash_decrypt_trlwe_device(idash_ctx *ctx, const int32_t
     if (st != IDASH_OK) return st;
     const uint8_t *in = static_cast<const uint8_t *>(d_in) + in_layout->payload_offset;
     if (k.binary && N % 32 == 0) {
-        // threads per row: 8 coefficients each, rounded up to whole warps
-        const uint32_t need = (num_samples + kBinCols - 1) / kBinCols;
-        const uint32_t row_threads = need <= 32 ? 32 : need <= 64 ? 64 : 128;  // need <= 2048 / kBinCols
+        // threads per row: kNegCols coefficients each, rounded up to whole warps
+        const uint32_t need = (num_samples + kNegCols - 1) / kNegCols;
+        const uint32_t row_threads = need <= 32 ? 32 : need <= 64 ? 64 : 128;  // need <= 2048 / kNegCols
         const uint32_t rows_per_cta = kDecryptThreads / row_threads;
-        const size_t smem = (size_t((N / 32 + 3) / 4 * 4) + size_t(rows_per_cta) * padded(2 * N)) * 4;
+        const size_t smem = (size_t(neg_mask_words(N)) + size_t(rows_per_cta) * neg_ext_words(N)) * 4;
         auto launch = [&](auto kernel) {
             // up to 8 rows of 2.25N words (144 KiB at N = 2048): above the default 48 KiB
             cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));

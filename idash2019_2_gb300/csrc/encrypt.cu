@@ -14,6 +14,7 @@
 
 #include "capi_internal.hpp"
 #include "common.cuh"
+#include "negacyclic.cuh"
 
 namespace idash {
 namespace {
@@ -46,6 +47,30 @@ struct EncArgs {
     int64_t var_off, hdr_off;
     int32_t *noise;  // optional [n_rows * N]
 };
+
+// Noise and message of coefficient j of row r, and the body word b[j].
+__device__ __forceinline__ void enc_finish(const EncArgs &a, uint64_t r, uint32_t j, uint32_t as_j, uint32_t *body) {
+    // noise: dtot32(alpha * z), z standard normal (Box-Muller)
+    const uint64_t ni = (r * a.N + j) * 2;
+    const float u1 = (float(enc_hash(a.key_e, ni) >> 8) + 0.5f) * 0x1p-24f;
+    const float u2 = float(enc_hash(a.key_e, ni + 1) >> 8) * 0x1p-24f;
+    const float z = sqrtf(-2.0f * logf(u1)) * cospif(2.0f * u2);
+    const int32_t e_j = int32_t(truncf(a.noise_scale * z));
+    // message: the one-hot value of the feature in this slot
+    uint32_t m = 0;
+    const uint32_t g = j / a.region_size, smp = j % a.region_size;
+    if (g < a.num_regions && smp < a.num_samples) {
+        const uint32_t src = a.slot_src[r * a.num_regions + g];
+        if (src != kNoSource) {
+            const uint32_t pi = src / 3, v = src % 3;
+            const int32_t gv = a.geno[uint64_t(pi) * a.geno_stride + smp];
+            if (gv == int32_t(v)) m = uint32_t(a.one);
+            else if (gv < 0 || gv > 2) m = uint32_t(a.nan[v]);
+        }
+    }
+    body[j] = as_j + uint32_t(e_j) + m;
+    if (a.noise) a.noise[r * a.N + j] = e_j;
+}
 
 // One CTA per row (grid-stride).  Shared memory: ext[2N], the negacyclic
 // extension of the fresh mask (ext[N + t] = a[t], ext[t] = -a[t]), then the
@@ -90,29 +115,55 @@ __global__ void __launch_bounds__(kEncThreads) k_encrypt_rows(const EncArgs a) {
             for (uint32_t c = 0; c < kEncCols; ++c) {
                 const uint32_t j = j0 + c * kEncThreads;
                 if (j >= N) continue;
-                // noise: dtot32(alpha * z), z standard normal (Box-Muller)
-                const uint64_t ni = (r * N + j) * 2;
-                const float u1 = (float(enc_hash(a.key_e, ni) >> 8) + 0.5f) * 0x1p-24f;
-                const float u2 = float(enc_hash(a.key_e, ni + 1) >> 8) * 0x1p-24f;
-                const float z = sqrtf(-2.0f * logf(u1)) * cospif(2.0f * u2);
-                const int32_t e_j = int32_t(truncf(a.noise_scale * z));
-                // message: the one-hot value of the feature in this slot
-                uint32_t m = 0;
-                const uint32_t g = j / a.region_size, smp = j % a.region_size;
-                if (g < a.num_regions && smp < a.num_samples) {
-                    const uint32_t src = a.slot_src[r * a.num_regions + g];
-                    if (src != kNoSource) {
-                        const uint32_t pi = src / 3, v = src % 3;
-                        const int32_t gv = a.geno[uint64_t(pi) * a.geno_stride + smp];
-                        if (gv == int32_t(v)) m = uint32_t(a.one);
-                        else if (gv < 0 || gv > 2) m = uint32_t(a.nan[v]);
-                    }
-                }
-                body[j] = acc[c] + uint32_t(e_j) + m;
-                if (a.noise) a.noise[r * N + j] = e_j;
+                enc_finish(a, r, j, acc[c], body);
             }
         }
         if (threadIdx.x == 0) {
+            if (a.hdr_off >= 0) {
+                *reinterpret_cast<uint32_t *>(rec + a.hdr_off) = a.row_index ? a.row_index[r] : uint32_t(r);
+                *reinterpret_cast<int32_t *>(rec + a.hdr_off + 4) = a.tag;
+            }
+            if (a.var_off >= 0) *reinterpret_cast<double *>(rec + a.var_off) = a.variance;
+        }
+    }
+}
+
+// Binary keys, N a multiple of 32: the register-windowed product of
+// negacyclic.cuh, kNegCols consecutive coefficients per thread, kRowsPerCta
+// rows per CTA, each with its own padded extension of its fresh mask.
+template <uint32_t kRowThreads>
+__global__ void __launch_bounds__(kEncThreads) k_encrypt_binary(const EncArgs a) {
+    constexpr uint32_t kRowsPerCta = kEncThreads / kRowThreads;
+    extern __shared__ __align__(16) uint32_t sh[];
+    const uint32_t N = a.N;
+    uint32_t *key_mask = sh;
+    uint32_t *ext_all = sh + neg_mask_words(N);  // kRowsPerCta padded extensions
+    neg_build_mask(key_mask, N, a.key_idx, a.n_nz);
+    const uint32_t sub = threadIdx.x / kRowThreads, x = threadIdx.x % kRowThreads;
+    const uint32_t j0 = kNegCols * x;
+    const uint32_t ext_words = neg_ext_words(N);
+    for (uint64_t r0 = uint64_t(blockIdx.x) * kRowsPerCta; r0 < a.n_rows; r0 += uint64_t(gridDim.x) * kRowsPerCta) {
+        __syncthreads();  // the previous rows are done with ext (and the key mask is complete)
+        for (uint32_t t = threadIdx.x; t < kRowsPerCta * N; t += blockDim.x) {
+            const uint32_t s = t / N, k = t % N;
+            const uint64_t r = r0 + s;
+            if (r >= a.n_rows) break;
+            const uint32_t v = enc_hash(a.key_a, r * N + k);
+            neg_store(ext_all + s * ext_words, N, k, v);
+            const uint64_t orow = a.row_out ? a.row_out[r] : r;
+            reinterpret_cast<uint32_t *>(a.out + orow * a.out_stride + a.payload_off)[k] = v;
+        }
+        __syncthreads();
+        const uint64_t r = r0 + sub;
+        if (r >= a.n_rows || j0 >= N) continue;
+        uint32_t acc[kNegCols];
+        neg_product(ext_all + sub * ext_words, N, j0, key_mask, acc);
+        const uint64_t orow = a.row_out ? a.row_out[r] : r;
+        uint8_t *rec = a.out + orow * a.out_stride;
+        uint32_t *body = reinterpret_cast<uint32_t *>(rec + a.payload_off) + N;
+#pragma unroll 4
+        for (uint32_t q = 0; q < kNegCols; ++q) enc_finish(a, r, j0 + q, acc[q], body);
+        if (x == 0) {
             if (a.hdr_off >= 0) {
                 *reinterpret_cast<uint32_t *>(rec + a.hdr_off) = a.row_index ? a.row_index[r] : uint32_t(r);
                 *reinterpret_cast<int32_t *>(rec + a.hdr_off + 4) = a.tag;
@@ -174,6 +225,33 @@ extern "C" idash_status idash_encrypt_trlwe_device(idash_ctx *ctx, const idash_e
     a.var_off = out_layout->variance_offset;
     a.hdr_off = out_layout->header_offset;
     a.noise = d_noise;
+    if (k.binary && p->N % 32 == 0) {
+        // threads per row: kNegCols coefficients each, rounded up to whole warps
+        const uint32_t need = p->N / kNegCols;
+        const uint32_t row_threads = need <= 32 ? 32 : need <= 64 ? 64 : 128;  // N <= 2048
+        const uint32_t rows_per_cta = kEncThreads / row_threads;
+        const size_t smem = (size_t(neg_mask_words(p->N)) + size_t(rows_per_cta) * neg_ext_words(p->N)) * 4;
+        auto launch = [&](auto kernel) {
+            // up to 8 rows of 2.25N words (144 KiB at N = 2048): above the default 48 KiB
+            cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+            int per_sm = 0;
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kEncThreads, smem) != cudaSuccess ||
+                per_sm < 1)
+                per_sm = 1;
+            const uint64_t ctas = (n_rows + rows_per_cta - 1) / rows_per_cta;
+            const uint32_t blocks = uint32_t(std::min<uint64_t>(ctas, uint64_t(ctx->sm_count) * per_sm));
+            kernel<<<blocks, kEncThreads, smem, s>>>(a);
+        };
+        switch (row_threads) {
+            case 32: launch(k_encrypt_binary<32>); break;
+            case 64: launch(k_encrypt_binary<64>); break;
+            default: launch(k_encrypt_binary<128>); break;
+        }
+        st = ctx->check_cuda(cudaGetLastError(), "k_encrypt_binary launch");
+        release_key(&k, s);
+        if (st == IDASH_OK) ctx->stats.kernel_launches++;
+        return st;
+    }
     const size_t smem = size_t(2) * p->N * 4 + size_t(a.n_nz) * 8;
     const uint32_t blocks = uint32_t(std::min<uint64_t>(n_rows, uint64_t(ctx->sm_count) * 8));
     if (k.binary)
