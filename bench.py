@@ -467,6 +467,51 @@ def section_serving(ctx, seed, n_requests=10000, budget=150 << 30, inflight=4):
                         "request ciphertexts generated on the device"}
 
 
+def section_files(seed, small=False):
+    """Rows f1/f2: the whole cloud step through its files (idash_cloud_files,
+    eval/cloud.cpp:3-28): params.bin, the model directory of one .hr file per
+    output (eval/idash.cpp:66-114), encrypted_data.bin in, and
+    encrypted_prediction.bin out, on the headline's shape (1,000 individuals,
+    16,184 tags, 80,882 targets x 3, 5 neighbours).  Three calls: parsing the
+    .hr files, the same writing the flattened-model cache, and reading the
+    cache.  Opt-in (about 2.5 GB of files in the temporary directory)."""
+    import shutil
+    import tempfile
+    from idash2019_2_gb300 import filesets, gpu
+    n_indiv, n_tags, n_targets = (1000, 2000, 10000) if small else (1000, 16184, 80882)
+    d = tempfile.mkdtemp(prefix="idash_cloud_files_")
+    try:
+        t0 = time.perf_counter()
+        info = filesets.write_cloud_inputs(d, seed, n_indiv, n_tags, n_targets, 5)
+        gen_s = time.perf_counter() - t0
+        paths = [os.path.join(d, x) for x in ("params.bin", "model", "encrypted_data.bin", "encrypted_prediction.bin")]
+        cache = os.path.join(d, "model.cache")
+        runs = {}
+        for name, use_cache in (("parse_model", False), ("parse_and_write_cache", True), ("model_from_cache", True)):
+            if use_cache:
+                os.environ["IDASH_MODEL_CACHE"] = cache
+            else:
+                os.environ.pop("IDASH_MODEL_CACHE", None)
+            t0 = time.perf_counter()
+            rep = gpu.cloud_files(*paths)
+            wall = time.perf_counter() - t0
+            runs[name] = {"wall_s": wall, **{k: rep[k] for k in ("read_s", "plan_s", "score_s", "write_s",
+                                                                   "model_from_cache")}}
+        os.environ.pop("IDASH_MODEL_CACHE", None)
+        out_bytes = os.path.getsize(paths[3])
+        in_bytes = os.path.getsize(paths[2])
+    finally:
+        shutil.rmtree(d, ignore_errors=True)
+    preds = info["outputs"] * n_indiv
+    best = runs["model_from_cache"]["wall_s"]
+    return {"value": preds / best, "unit": UNIT, "s_per_step": best,
+            "workload": f"cloud step on files: {n_indiv:,} individuals x {n_targets:,} targets x 3, {n_tags:,} tags, "
+                        "5 neighbours (one .hr file per output), wall time of idash_cloud_files",
+            "files": {"model_files": info["outputs"], "model_terms": info["terms"], "encrypted_data_bytes": in_bytes,
+                      "encrypted_prediction_bytes": out_bytes, "generate_s": gen_s},
+            "runs": runs}
+
+
 def run_sections(ctx, args, sections):
     """The forms beside the headline.  --small shrinks the LWE forms to
     100 individuals x 2,000 tags x 10,000 targets (a few GB on the device),
@@ -485,6 +530,8 @@ def run_sections(ctx, args, sections):
         forms["intpoly"] = section_intpoly(ctx, args.seed + 3, scale=64 if args.small else 1)
     if "serving" in sections:
         forms["serving"] = section_serving(ctx, args.seed + 2)
+    if "files" in sections:
+        forms["files"] = section_files(args.seed + 4, small=args.small)
     return forms
 
 
@@ -647,7 +694,8 @@ def main():
     ap.add_argument("--seed", type=int, default=0x1DA52019)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--sections", default="plain,kinds,encrypt,decrypt,lwe_full,batched_uneven,intpoly,serving",
-                    help="extra forms measured after the headline (comma list, '' for none)")
+                    help="extra forms measured after the headline (comma list, '' for none; 'files', the "
+                         "cloud step through its files, is opt-in)")
     ap.add_argument("--no-headline", action="store_true",
                     help="measure only --sections (no headline, e2e or CPU baseline)")
     ap.add_argument("--small", action="store_true", help="LWE sections at a reduced size (profiling)")

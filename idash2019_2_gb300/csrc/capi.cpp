@@ -3,6 +3,7 @@
 #include <algorithm>
 #include <cstring>
 #include <string>
+#include <thread>
 
 #include "capi_internal.hpp"
 
@@ -79,8 +80,15 @@ uint32_t row_words_of(const idash_model *m, uint32_t n_indiv) {
     return m->form == Form::kTrlwe ? 2 * m->tp.N : n_indiv * (m->lp.n + 1);
 }
 
-idash_status build_and_upload(idash_model *m, const Candidate &c) {
-    idash_ctx *ctx = m->ctx;
+// A candidate's plan, built on the host only (safe to run on several threads
+// at once: it reads the model's arrays and writes nothing shared).
+struct BuiltPlan {
+    Plan plan;
+    std::string err;
+    bool index_error = false;
+};
+
+BuiltPlan make_plan(const idash_model *m, const Candidate &c) {
     PlanInput in;
     in.form = m->form;
     in.n_out = m->n_out;
@@ -106,12 +114,18 @@ idash_status build_and_upload(idash_model *m, const Candidate &c) {
     // batched kinds split neighbourhoods larger than one window into parts
     // (later launches accumulate); the direct kernel reads global memory
     lim.split = c.split && c.kind != KernelKind::kDirect;
-    Plan plan;
-    bool index_error = false;
-    const std::string err = build_plan(in, lim, &plan, &index_error);
-    if (!err.empty()) return ctx->fail(index_error ? IDASH_ERR_INDEX : IDASH_ERR_UNSUPPORTED, err);
-    if (plan.blocks.size() >= 0xFFFFFFFFull || plan.terms.size() >= 0xFFFFFFFFull)
-        return ctx->fail(IDASH_ERR_UNSUPPORTED, "model too large for 32-bit plan indices");
+    BuiltPlan b;
+    b.err = build_plan(in, lim, &b.plan, &b.index_error);
+    if (b.err.empty() && (b.plan.blocks.size() >= 0xFFFFFFFFull || b.plan.terms.size() >= 0xFFFFFFFFull))
+        b.err = "model too large for 32-bit plan indices";
+    return b;
+}
+
+// Makes a built plan the model's: device arrays, kernel shape, CTAs.
+idash_status upload_plan(idash_model *m, const Candidate &c, BuiltPlan &&b) {
+    idash_ctx *ctx = m->ctx;
+    if (!b.err.empty()) return ctx->fail(b.index_error ? IDASH_ERR_INDEX : IDASH_ERR_UNSUPPORTED, b.err);
+    Plan plan = std::move(b.plan);
     m->drop_graph();
     m->free_device();
     idash_status s;
@@ -146,6 +160,9 @@ idash_status build_and_upload(idash_model *m, const Candidate &c) {
     m->ctas = uint32_t(ctx->sm_count) * std::max<uint32_t>(cps, 1);
     return IDASH_OK;
 }
+
+idash_status build_and_upload(idash_model *m, const Candidate &c) { return upload_plan(m, c, make_plan(m, c)); }
+
 
 ScoreArgs make_args(idash_model *m, const uint8_t *in_payload, uint64_t in_stride, uint8_t *out_payload,
                     uint64_t out_stride, uint32_t row_words, uint32_t b_lo, uint32_t b_hi, uint64_t out_lo,
@@ -349,6 +366,49 @@ idash_status plan_default(idash_model *m) {
 }
 
 bool autotune_wanted(idash_model *m) { return !m->tuned && m->ctx->opt_kernel != 1 && candidates(m).size() > 1; }
+
+// Autotuning: the candidates' plans are built on host threads, up to
+// kPlanThreads at a time, then each is uploaded and timed in order by
+// time_fn (milliseconds per unit, <= 0 when it failed).  Split candidates
+// are tried only when no whole one worked.  The fastest becomes the model's
+// plan (or the first feasible one, when none could be timed).
+constexpr size_t kPlanThreads = 8;
+
+template <typename TimeFn>
+idash_status autotune(idash_model *m, TimeFn time_fn) {
+    const std::vector<Candidate> cands = candidates(m);
+    float best = -1.f;
+    Candidate best_c{};
+    BuiltPlan best_plan;
+    bool stop = false;
+    for (size_t i = 0; i < cands.size() && !stop; i += kPlanThreads) {
+        const size_t n = std::min(kPlanThreads, cands.size() - i);
+        std::vector<BuiltPlan> built(n);
+        std::vector<std::thread> threads;
+        for (size_t k = 0; k < n; ++k)
+            threads.emplace_back([&, k] { built[k] = make_plan(m, cands[i + k]); });
+        for (auto &t : threads) t.join();
+        for (size_t k = 0; k < n; ++k) {
+            const Candidate &c = cands[i + k];
+            if (c.split && best >= 0) {
+                stop = true;
+                break;
+            }
+            BuiltPlan keep;
+            if (built[k].err.empty()) keep.plan = built[k].plan;  // the host copy, kept if this one wins
+            if (upload_plan(m, c, std::move(built[k])) != IDASH_OK) continue;
+            const float ms = time_fn();
+            if (ms > 0 && (best < 0 || ms < best)) {
+                best = ms;
+                best_c = c;
+                best_plan = std::move(keep);
+            }
+        }
+    }
+    idash_status s = best < 0 ? plan_default(m) : upload_plan(m, best_c, std::move(best_plan));
+    if (s == IDASH_OK) m->tuned = true;
+    return s;
+}
 
 }  // namespace
 
@@ -724,23 +784,7 @@ idash_status idash_score_trlwe_device(idash_model *m, const void *d_in, const id
     }
     if (autotune_wanted(m)) {
         // Autotune on the caller's buffers: plan every candidate, time it, keep the best.
-        float best = -1.f;
-        Candidate best_c{};
-        for (const Candidate &c : candidates(m)) {
-            if (c.split && best >= 0) break;
-            if (build_and_upload(m, c) != IDASH_OK) continue;
-            const float ms = time_candidate(m, d_in, il, d_out, ol, cs, 3);
-            if (ms > 0 && (best < 0 || ms < best)) {
-                best = ms;
-                best_c = c;
-            }
-        }
-        if (best < 0) {
-            if ((s = plan_default(m)) != IDASH_OK) return s;
-        } else if ((s = build_and_upload(m, best_c)) != IDASH_OK) {
-            return s;
-        }
-        m->tuned = true;
+        if ((s = autotune(m, [&]() { return time_candidate(m, d_in, il, d_out, ol, cs, 3); })) != IDASH_OK) return s;
     }
     if (ctx->opt_graph) {
         if (!(m->graph && m->g_in == d_in && m->g_out == d_out && same_layout(m->g_in_layout, *il) &&
@@ -993,32 +1037,18 @@ idash_status idash_score_lwe_device(idash_model *m, uint32_t n_indiv, const int3
         if ((s = ctx->check_cuda(cudaStreamWaitEvent(cs, ctx->join_in, 0), "join")) != IDASH_OK) return s;
     }
     if (autotune_wanted(m)) {
-        // tune on (at most) the first ~64 phase-0 blocks of this range
-        uint32_t b_lo, b_hi;
-        float best = -1.f;
-        Candidate best_c{};
-        for (const Candidate &c : candidates(m)) {
-            if (c.split && best >= 0) break;
-            if (build_and_upload(m, c) != IDASH_OK) continue;
+        // tune on (at most) the first ~64 phase-0 blocks of this range, per output
+        s = autotune(m, [&]() -> float {
+            uint32_t b_lo, b_hi;
             block_range(m, 0, out_begin, out_end, &b_lo, &b_hi);
-            if (b_hi == b_lo) continue;
+            if (b_hi == b_lo) return -1.f;
             const uint32_t hi = std::min<uint32_t>(b_hi, b_lo + 64);
             const uint64_t o_hi = std::min<uint64_t>(out_end, m->plan.blocks[hi - 1].out_hi);
             const float ms = time_candidate_lwe(m, n_indiv, d_in, in_row_stride, out_begin, o_hi, d_out,
                                                 out_row_stride, cs, 2);
-            if (ms <= 0) continue;
-            const float per_out = ms / float(o_hi - out_begin);
-            if (best < 0 || per_out < best) {
-                best = per_out;
-                best_c = c;
-            }
-        }
-        if (best < 0) {
-            if ((s = plan_default(m)) != IDASH_OK) return s;
-        } else if ((s = build_and_upload(m, best_c)) != IDASH_OK) {
-            return s;
-        }
-        m->tuned = true;
+            return ms <= 0 ? -1.f : ms / float(o_hi - out_begin);
+        });
+        if (s != IDASH_OK) return s;
     }
     const uint32_t rw = row_words_of(m, n_indiv);
     const uint32_t n_slices = (rw + m->slice_words - 1) / m->slice_words;
