@@ -394,14 +394,12 @@ idash_status autotune(idash_model *m, TimeFn time_fn) {
                 stop = true;
                 break;
             }
-            BuiltPlan keep;
-            if (built[k].err.empty()) keep.plan = built[k].plan;  // the host copy, kept if this one wins
             if (upload_plan(m, c, std::move(built[k])) != IDASH_OK) continue;
             const float ms = time_fn();
             if (ms > 0 && (best < 0 || ms < best)) {
                 best = ms;
                 best_c = c;
-                best_plan = std::move(keep);
+                best_plan.plan = std::move(m->plan);  // the next upload replaces the model's plan anyway
             }
         }
     }
