@@ -492,6 +492,8 @@ def section_files(seed, small=False):
                 os.environ["IDASH_MODEL_CACHE"] = cache
             else:
                 os.environ.pop("IDASH_MODEL_CACHE", None)
+            if os.path.exists(paths[3]):
+                os.remove(paths[3])  # each run writes a new prediction file (no truncation of the last)
             t0 = time.perf_counter()
             rep = gpu.cloud_files(*paths)
             wall = time.perf_counter() - t0

@@ -367,12 +367,12 @@ idash_status plan_default(idash_model *m) {
 
 bool autotune_wanted(idash_model *m) { return !m->tuned && m->ctx->opt_kernel != 1 && candidates(m).size() > 1; }
 
-// Autotuning: the candidates' plans are built on host threads, up to
-// kPlanThreads at a time, then each is uploaded and timed in order by
+// Autotuning: the candidates' plans are built on host threads, one per
+// host core up to kPlanThreads at a time, then each is uploaded and timed in order by
 // time_fn (milliseconds per unit, <= 0 when it failed).  Split candidates
 // are tried only when no whole one worked.  The fastest becomes the model's
 // plan (or the first feasible one, when none could be timed).
-constexpr size_t kPlanThreads = 8;
+constexpr size_t kPlanThreads = 16;
 
 template <typename TimeFn>
 idash_status autotune(idash_model *m, TimeFn time_fn) {
@@ -381,8 +381,9 @@ idash_status autotune(idash_model *m, TimeFn time_fn) {
     Candidate best_c{};
     BuiltPlan best_plan;
     bool stop = false;
-    for (size_t i = 0; i < cands.size() && !stop; i += kPlanThreads) {
-        const size_t n = std::min(kPlanThreads, cands.size() - i);
+    const size_t width = std::max<size_t>(1, std::min<size_t>(kPlanThreads, std::thread::hardware_concurrency()));
+    for (size_t i = 0; i < cands.size() && !stop; i += width) {
+        const size_t n = std::min(width, cands.size() - i);
         std::vector<BuiltPlan> built(n);
         std::vector<std::thread> threads;
         for (size_t k = 0; k < n; ++k)

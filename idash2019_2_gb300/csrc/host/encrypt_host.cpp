@@ -187,12 +187,7 @@ Status encrypt_data(EncryptedData &enc, const PlaintextData &plain, const IdashK
 }
 
 Status write_encrypted_data(const EncryptedData &enc, const std::string &filename) {
-    FILE *f = std::fopen(filename.c_str(), "wb");
-    if (!f) return Status::Err(IDASH_ERR_IO, "cannot open '" + filename + "' for write");
-    const size_t put = enc.image.data ? std::fwrite(enc.image.data, 1, enc.image.bytes, f) : 0;
-    const bool ok = std::fclose(f) == 0 && put == enc.image.bytes;
-    if (!ok) return Status::Err(IDASH_ERR_IO, "short write to '" + filename + "'");
-    return Status::Ok();
+    return write_image_file(enc.image.data, enc.image.bytes, filename);
 }
 
 }  // namespace idash_host

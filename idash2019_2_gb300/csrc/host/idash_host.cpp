@@ -3,12 +3,20 @@
 
 #include <cuda_runtime.h>
 
+#include <fcntl.h>
+#include <sys/stat.h>
+#include <unistd.h>
+
 #include <algorithm>
+#include <atomic>
+#include <cerrno>
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <fstream>
+#include <thread>
+#include <vector>
 
 namespace idash_host {
 
@@ -190,29 +198,55 @@ Status read_model(Model &model, const IdashParams &params, const std::string &pa
     return Status::Ok();
 }
 
+// Reads (or writes) bytes [off, off + bytes) of fd into (from) buf: a
+// record image is one contiguous range, so up to 8 threads each move a
+// slice of it with pread/pwrite (one thread below 64 MiB a slice).
+static bool parallel_io(int fd, uint8_t *buf, size_t bytes, uint64_t off, bool write) {
+    constexpr size_t kSlice = size_t(64) << 20;
+    const size_t n_threads = std::max<size_t>(1, std::min<size_t>(8, bytes / kSlice));
+    std::atomic<bool> ok{true};
+    auto run = [&](size_t t) {
+        const size_t lo = bytes * t / n_threads, hi = bytes * (t + 1) / n_threads;
+        for (size_t done = lo; done < hi && ok.load();) {
+            const ssize_t r = write ? ::pwrite(fd, buf + done, hi - done, off_t(off + done))
+                                    : ::pread(fd, buf + done, hi - done, off_t(off + done));
+            if (r < 0 && errno == EINTR) continue;
+            if (r <= 0) {
+                ok = false;
+                break;
+            }
+            done += size_t(r);
+        }
+    };
+    std::vector<std::thread> threads;
+    for (size_t t = 1; t < n_threads; ++t) threads.emplace_back(run, t);
+    run(0);
+    for (auto &th : threads) th.join();
+    return ok.load();
+}
+
 static Status read_image(RecordImage &img, const std::string &filename) {
-    FILE *f = std::fopen(filename.c_str(), "rb");
-    if (!f) return Status::Err(IDASH_ERR_IO, "cannot open '" + filename + "'");
+    const int fd = ::open(filename.c_str(), O_RDONLY);
+    if (fd < 0) return Status::Err(IDASH_ERR_IO, "cannot open '" + filename + "'");
+    struct stat sb {};
     uint64_t count = 0;
-    if (std::fread(&count, 8, 1, f) != 1) {
-        std::fclose(f);
+    if (::fstat(fd, &sb) != 0 || sb.st_size < 8 || ::pread(fd, &count, 8, 0) != 8) {
+        ::close(fd);
         return Status::Err(IDASH_ERR_FORMAT, "'" + filename + "': missing record count");
     }
-    std::fseek(f, 0, SEEK_END);
-    const long size = std::ftell(f);
-    std::fseek(f, 0, SEEK_SET);
-    if (size < 8 || uint64_t(size) != 8 + count * kRecordBytes) {
-        std::fclose(f);
+    const uint64_t size = uint64_t(sb.st_size);
+    if (count > (size - 8) / kRecordBytes || size != 8 + count * kRecordBytes) {
+        ::close(fd);
         return Status::Err(IDASH_ERR_FORMAT, "'" + filename + "': size is not 8 + count * 8208");
     }
     idash_status s = img.allocate(count);
     if (s != IDASH_OK) {
-        std::fclose(f);
+        ::close(fd);
         return Status::Err(s, "cannot allocate the record image");
     }
-    const size_t got = std::fread(img.data, 1, size_t(size), f);
-    std::fclose(f);
-    if (got != size_t(size)) return Status::Err(IDASH_ERR_IO, "'" + filename + "': short read");
+    const bool ok = parallel_io(fd, img.data, size_t(size), 0, false);
+    ::close(fd);
+    if (!ok) return Status::Err(IDASH_ERR_IO, "'" + filename + "': short read");
     return Status::Ok();
 }
 
@@ -242,13 +276,17 @@ Status read_encrypted_predictions(EncryptedPredictions &preds, const std::string
     return Status::Ok();
 }
 
-Status write_encrypted_predictions(const EncryptedPredictions &preds, const std::string &filename) {
-    FILE *f = std::fopen(filename.c_str(), "wb");
-    if (!f) return Status::Err(IDASH_ERR_IO, "cannot open '" + filename + "' for write");
-    const size_t put = preds.image.data ? std::fwrite(preds.image.data, 1, preds.image.bytes, f) : 0;
-    const bool ok = std::fclose(f) == 0 && put == preds.image.bytes;
+Status write_image_file(const uint8_t *data, uint64_t bytes, const std::string &filename) {
+    const int fd = ::open(filename.c_str(), O_WRONLY | O_CREAT | O_TRUNC, 0644);
+    if (fd < 0) return Status::Err(IDASH_ERR_IO, "cannot open '" + filename + "' for write");
+    bool ok = data && parallel_io(fd, const_cast<uint8_t *>(data), size_t(bytes), 0, true);
+    ok = ::close(fd) == 0 && ok;
     if (!ok) return Status::Err(IDASH_ERR_IO, "short write to '" + filename + "'");
     return Status::Ok();
+}
+
+Status write_encrypted_predictions(const EncryptedPredictions &preds, const std::string &filename) {
+    return write_image_file(preds.image.data, preds.image.bytes, filename);
 }
 
 FlatModel flatten_model(const Model &model) {

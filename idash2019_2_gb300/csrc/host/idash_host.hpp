@@ -88,9 +88,11 @@ Status write_params(const IdashParams &params, const std::string &filename);
 // eval/parse_vw.cpp:8-30).
 Status read_model(Model &model, const IdashParams &params, const std::string &path);
 // encrypted_data.bin / encrypted_prediction.bin (eval/idash.cpp:513-613):
-// one bulk read / write of the whole image.
+// the whole image moves as one range of the file.
 Status read_encrypted_data(EncryptedData &data, const IdashParams &params, const std::string &filename);
 Status write_encrypted_predictions(const EncryptedPredictions &preds, const std::string &filename);
+// Writes a whole record image to `filename` (created or truncated).
+Status write_image_file(const uint8_t *data, uint64_t bytes, const std::string &filename);
 Status read_encrypted_predictions(EncryptedPredictions &preds, const std::string &filename);
 
 struct CloudTiming {
