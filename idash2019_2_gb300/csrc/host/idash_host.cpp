@@ -172,28 +172,60 @@ Status write_params(const IdashParams &params, const std::string &filename) {
 }
 
 Status read_model(Model &model, const IdashParams &params, const std::string &path) {
-    for (const auto &elem : params.out_features_index) {
-        const uint64_t pos = elem.first;
-        for (uint32_t snp = 0; snp < 3; ++snp) {
-            std::unordered_map<std::string, int32_t> coefs;
-            Status st = read_hr(path + "/" + std::to_string(pos) + "_" + std::to_string(snp) + ".hr", &coefs);
-            if (!st.ok()) return st;
-            auto &mc = model.model[elem.second[snp]] = std::unordered_map<FeatBigIndex, int32_t>();
-            for (const auto &c : coefs) {
-                if (c.first == "Constant") {
-                    mc[IdashParams::constant_bigIndex()] = c.second;
-                    continue;
-                }
-                uint64_t in_pos;
-                uint32_t in_snp;
-                if (!split_feature(c.first, &in_pos, &in_snp))
-                    return Status::Err(IDASH_ERR_FORMAT, "model: bad feature name '" + c.first + "'");
-                const auto it = params.in_features_index.find(in_pos);
-                if (it == params.in_features_index.end() || in_snp >= 3)
-                    return Status::Err(IDASH_ERR_INDEX, "model: feature '" + c.first + "' is not a tag SNP of params");
-                mc[it->second[in_snp]] = c.second;
+    // The files are read and parsed on host threads, each into its terms in
+    // the iteration order of its name -> coefficient map (what the reference
+    // iterates); the model's maps are then filled on this thread in the
+    // reference's order, so every unordered_map sees the same insertions.
+    struct File {
+        FeatBigIndex out;
+        std::string name;
+        std::vector<std::pair<FeatBigIndex, int32_t>> terms;
+        Status st = Status::Ok();
+    };
+    std::vector<File> files;
+    files.reserve(params.out_features_index.size() * 3);
+    for (const auto &elem : params.out_features_index)
+        for (uint32_t snp = 0; snp < 3; ++snp)
+            files.push_back(File{elem.second[snp],
+                                 path + "/" + std::to_string(elem.first) + "_" + std::to_string(snp) + ".hr", {}});
+    auto parse = [&](File &f) {
+        std::unordered_map<std::string, int32_t> coefs;
+        f.st = read_hr(f.name, &coefs);
+        if (!f.st.ok()) return;
+        f.terms.reserve(coefs.size());
+        for (const auto &c : coefs) {
+            if (c.first == "Constant") {
+                f.terms.emplace_back(IdashParams::constant_bigIndex(), c.second);
+                continue;
             }
+            uint64_t in_pos;
+            uint32_t in_snp;
+            if (!split_feature(c.first, &in_pos, &in_snp)) {
+                f.st = Status::Err(IDASH_ERR_FORMAT, "model: bad feature name '" + c.first + "'");
+                return;
+            }
+            const auto it = params.in_features_index.find(in_pos);
+            if (it == params.in_features_index.end() || in_snp >= 3) {
+                f.st = Status::Err(IDASH_ERR_INDEX, "model: feature '" + c.first + "' is not a tag SNP of params");
+                return;
+            }
+            f.terms.emplace_back(it->second[in_snp], c.second);
         }
+    };
+    const size_t n_threads =
+        std::max<size_t>(1, std::min<size_t>({16, std::thread::hardware_concurrency(), files.size() / 256 + 1}));
+    std::vector<std::thread> threads;
+    for (size_t t = 1; t < n_threads; ++t)
+        threads.emplace_back([&, t] {
+            for (size_t i = files.size() * t / n_threads; i < files.size() * (t + 1) / n_threads; ++i) parse(files[i]);
+        });
+    for (size_t i = 0; i < files.size() / n_threads; ++i) parse(files[i]);
+    for (auto &th : threads) th.join();
+    for (File &f : files) {
+        if (!f.st.ok()) return f.st;  // the first failure in the reference's reading order
+        auto &mc = model.model[f.out] = std::unordered_map<FeatBigIndex, int32_t>();
+        for (const auto &t : f.terms) mc[t.first] = t.second;
+        std::vector<std::pair<FeatBigIndex, int32_t>>().swap(f.terms);
     }
     return Status::Ok();
 }
