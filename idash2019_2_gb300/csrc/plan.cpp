@@ -230,8 +230,15 @@ std::string build_plan(const PlanInput &in, const PlanLimits &lim, Plan *plan, b
             const G &first = groups[order[gi]], &last = groups[order[gend - 1]];
             b.out_lo = uint32_t(first.o0);
             b.out_hi = uint32_t(last.o0 + last.n);
-            for (size_t q = gi; q < gend; ++q) {
-                const G &g = groups[order[q]];
+            // the block's groups, most terms first: kernels that hand groups
+            // out dynamically then start the long ones early (longest
+            // processing time first), and the short ones fill in around them
+            std::vector<uint32_t> in_block(order.begin() + gi, order.begin() + gend);
+            std::stable_sort(in_block.begin(), in_block.end(), [&](uint32_t x, uint32_t y) {
+                return groups[x].keys.size() > groups[y].keys.size();
+            });
+            for (const uint32_t gq : in_block) {
+                const G &g = groups[gq];
                 PlanGroup pg{};
                 pg.term_begin = uint32_t(plan->terms.size()) - b.term_begin;
                 pg.n_terms = uint32_t(g.keys.size());
