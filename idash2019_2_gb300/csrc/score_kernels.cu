@@ -201,7 +201,12 @@ __device__ __forceinline__ void accumulate_group(uint32_t (&acc)[G][4 * Q], cons
                 }
         }
         const uint32_t tend = taddr + 16 * gr.n_terms;
-#pragma unroll 2
+        // terms in flight per thread: two at four quads (measured best there).
+        // One quad carries little arithmetic per pair of dependent loads (term,
+        // then window), so more terms go in flight: on the uneven LWE form
+        // (128-word slices) unroll 2 / 4 / 8 / 16 ran 1.74 / 1.58 / 1.55 / 1.53 s
+        constexpr int kUnroll = Q == 1 ? 16 : 2;
+#pragma unroll kUnroll
         for (taddr += 16; taddr != tend; taddr += 16) {
             const uint4 tv = lds_v4(taddr);
             const uint32_t w = wbase + tv.w * (W * 4);
