@@ -853,11 +853,11 @@ idash_status idash_score_trlwe_host(idash_model *m, const void *h_in, const idas
     }
     uint8_t *d_in = ctx->d_in_buf + in_shift;
     uint8_t *d_out = ctx->d_out_buf + out_shift;
-    const uint8_t *hi = static_cast<const uint8_t *>(h_in);
-    uint8_t *ho = static_cast<uint8_t *>(h_out);
+    const uint8_t *host_in = static_cast<const uint8_t *>(h_in);
+    uint8_t *host_out = static_cast<uint8_t *>(h_out);
     if (autotune_wanted(m)) {
         // tune once on the device copies of this call's inputs
-        if ((s = ctx->check_cuda(cudaMemcpyAsync(d_in, hi, in_bytes, cudaMemcpyHostToDevice, ctx->stream), "h2d")) !=
+        if ((s = ctx->check_cuda(cudaMemcpyAsync(d_in, host_in, in_bytes, cudaMemcpyHostToDevice, ctx->stream), "h2d")) !=
             IDASH_OK)
             return s;
         if ((s = idash_score_trlwe_device(m, d_in, il, d_out, ol, nullptr)) != IDASH_OK) return s;
@@ -888,7 +888,7 @@ idash_status idash_score_trlwe_host(idash_model *m, const void *h_in, const idas
             // send the rows in [rows_sent, need) plus a lookahead of the next chunk's share
             uint64_t upto = std::min<uint64_t>(n_in_rows, std::max<uint64_t>(need, rows_sent + (n_in_rows + n_chunks - 1) / n_chunks));
             if (c == n_chunks - 1) upto = std::max<uint64_t>(upto, need);
-            s = ctx->check_cuda(cudaMemcpyAsync(d_in + rows_sent * il->row_stride, hi + rows_sent * il->row_stride,
+            s = ctx->check_cuda(cudaMemcpyAsync(d_in + rows_sent * il->row_stride, host_in + rows_sent * il->row_stride,
                                                 (upto - rows_sent) * il->row_stride, cudaMemcpyHostToDevice, ctx->h2d),
                                 "h2d chunk");
             if (s != IDASH_OK) return s;
@@ -927,7 +927,7 @@ idash_status idash_score_trlwe_host(idash_model *m, const void *h_in, const idas
         cudaEvent_t e = ctx->event(ev++);
         cudaEventRecord(e, ctx->stream);
         cudaStreamWaitEvent(ctx->d2h, e, 0);
-        s = ctx->check_cuda(cudaMemcpyAsync(ho + o_lo * ol->row_stride, d_out + o_lo * ol->row_stride,
+        s = ctx->check_cuda(cudaMemcpyAsync(host_out + o_lo * ol->row_stride, d_out + o_lo * ol->row_stride,
                                             (o_hi - o_lo) * ol->row_stride, cudaMemcpyDeviceToHost, ctx->d2h),
                             "d2h chunk");
         if (s != IDASH_OK) return s;

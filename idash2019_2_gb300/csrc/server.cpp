@@ -207,8 +207,6 @@ extern "C" idash_status idash_serve_trlwe(idash_model *m, const idash_serve_conf
             uint8_t *out0 = in0 + sh.blocks * sh.in_bytes_per_block;
             for (uint32_t b = 0; b < sh.blocks && st == IDASH_OK; ++b) {
                 const uint32_t ns = std::min<uint32_t>(RS, r.n_indiv - b * RS);
-                idash_trlwe_params p = m->tp;
-                p.num_samples = ns;
                 uint8_t *in_b = in0 + b * sh.in_bytes_per_block;
                 uint8_t *out_b = out0 + b * sh.out_bytes_per_block;
                 st = ctx->check_cuda(fill_uniform_rows(request_block_seed(r.seed, b), sh.row_begin,
