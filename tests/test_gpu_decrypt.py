@@ -134,3 +134,26 @@ def test_decrypt_errors(ctx):
     with pytest.raises(gpu.IdashError):
         gpu.decrypt_device(ctx, key[:1000], d.ptr, gpu.DENSE_TRLWE, 1, 10, d.ptr)  # N not a power of two
     d.free()
+
+
+@pytest.mark.parametrize("N", [4, 16, 32, 64, 256, 2048])
+def test_decrypt_polynomial_sizes(ctx, oracle, N):
+    """Every polynomial size the entry point takes, binary keys: N a multiple
+    of 32 runs the register-windowed kernel (1, 2, 4 or 8 rows per CTA by
+    the number of samples), N = 4 and 16 the general one; bit-exact."""
+    rng = np.random.default_rng(N)
+    n_rows = 37
+    rows = rng.integers(0, 2 ** 32, size=(n_rows, 2 * N), dtype=np.uint64).astype(np.uint32).view(np.int32)
+    key = rng.integers(0, 2, size=N).astype(np.int32)
+    d_in = ctx.device_alloc(rows.nbytes)
+    d_in.upload(rows)
+    lay = gpu.RowLayout(2 * N * 4, 0, -1, -1)
+    for ns in sorted({1, min(N, 17), N // 2 + 1, N}):
+        d_out = ctx.device_alloc(n_rows * ns * 4)
+        gpu.decrypt_device(ctx, key, d_in.ptr, lay, n_rows, ns, d_out.ptr)
+        ctx.sync()
+        got = d_out.download(dtype=np.float32).reshape(n_rows, ns)
+        want = oracle.trlwe_decrypt(rows, key, ns)
+        np.testing.assert_array_equal(got.view(np.uint32), want.view(np.uint32), err_msg=f"N={N} ns={ns}")
+        d_out.free()
+    d_in.free()

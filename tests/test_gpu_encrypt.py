@@ -136,3 +136,40 @@ def test_encrypt_cli_is_reproducible_with_a_seed(tmp_path):
     assert "encrypt wall time" in r.stdout
     gpu.encrypt_files(str(tmp_path / "keys.bin"), os.path.join(d, "tags.txt"), str(tmp_path / "api.bin"), seed=31337)
     assert filecmp.cmp(tmp_path / "encrypted_data.bin", tmp_path / "api.bin", shallow=False)
+
+
+@pytest.mark.parametrize("n", [16, 32, 256, 2048])
+def test_encrypt_polynomial_sizes(ctx, oracle, n):
+    """Fresh encryptions at other polynomial sizes (binary keys: N a multiple
+    of 32 runs the register-windowed kernel, N = 16 the general one): the
+    mask is the documented stream and b - a*s - m equals the reported noise."""
+    rng = np.random.default_rng(n)
+    ns, n_rows, seed = min(n, 20), 9, 777
+    key = rng.integers(0, 2, size=n).astype(np.int32)
+    geno = rng.integers(-1, 3, size=(3, ns)).astype(np.int8)
+    slot_src = np.array([0, 4, 8, 0xFFFFFFFF, 2, 5, 7, 1, 3], np.uint32)
+    d_src, d_geno = ctx.device_alloc(slot_src.nbytes), ctx.device_alloc(geno.nbytes)
+    d_src.upload(slot_src)
+    d_geno.upload(geno)
+    d_out = ctx.device_alloc(n_rows * 2 * n * 4)
+    d_noise = ctx.device_alloc(n_rows * n * 4)
+    params = gpu.encrypt_params(ns, 1, n, N=n)
+    gpu.encrypt_device(ctx, params, key, seed, n_rows, d_src.ptr, d_geno.ptr, ns, d_out.ptr,
+                       gpu.RowLayout(2 * n * 4, 0, -1, -1), d_noise=d_noise.ptr)
+    ctx.sync()
+    rows = d_out.download(dtype=np.int32).reshape(n_rows, 2 * n)
+    noise = d_noise.download(dtype=np.int32).reshape(n_rows, n)
+    for r in range(n_rows):
+        a = rows[r, :n].view(np.uint32)
+        mask = np.array([oracle.lib().oracle_hash32(seed, 21, r * n + j) for j in range(n)], np.uint32)
+        np.testing.assert_array_equal(a, mask)
+        msg = np.zeros(n, np.uint32)
+        if slot_src[r] != 0xFFFFFFFF:
+            p, v = divmod(int(slot_src[r]), 3)
+            gv = geno[p]
+            val = np.where(gv == v, params.one_t32, np.where((gv < 0) | (gv > 2), params.nan_t32[v], 0))
+            msg[:ns] = val.astype(np.int64).astype(np.uint32)
+        ph = (rows[r, n:].view(np.uint32) - oracle.negacyclic_mul(key, a)).astype(np.uint32)
+        np.testing.assert_array_equal((ph - msg).astype(np.uint32).view(np.int32), noise[r])
+    for b in (d_src, d_geno, d_out, d_noise):
+        b.free()
