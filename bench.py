@@ -468,13 +468,17 @@ def section_serving(ctx, seed, n_requests=10000, budget=150 << 30, inflight=4):
 
 
 def section_files(seed, small=False):
-    """Rows f1/f2: the whole cloud step through its files (idash_cloud_files,
-    eval/cloud.cpp:3-28): params.bin, the model directory of one .hr file per
-    output (eval/idash.cpp:66-114), encrypted_data.bin in, and
-    encrypted_prediction.bin out, on the headline's shape (1,000 individuals,
-    16,184 tags, 80,882 targets x 3, 5 neighbours).  Three calls: parsing the
-    .hr files, the same writing the flattened-model cache, and reading the
-    cache.  Opt-in (about 2.5 GB of files in the temporary directory)."""
+    """Rows f1-f4 on files, at the headline's shape (1,000 individuals, 16,184
+    tags, 80,882 targets x 3, 5 neighbours):
+      - the whole cloud step (idash_cloud_files, eval/cloud.cpp:3-28):
+        params.bin, the model directory of one .hr file per output
+        (eval/idash.cpp:66-114) and encrypted_data.bin in,
+        encrypted_prediction.bin out; three calls: parsing the .hr files, the
+        same writing the flattened-model cache, and reading the cache;
+      - party A's encryption of the tag genotypes (idash_encrypt_files,
+        eval/encrypt.cpp:14-38) and decryption of the predictions to the CSV
+        (idash_decrypt_files, eval/decrypt.cpp:13-48).
+    Opt-in (about 6 GB of files in the temporary directory)."""
     import shutil
     import tempfile
     from idash2019_2_gb300 import filesets, gpu
@@ -482,7 +486,7 @@ def section_files(seed, small=False):
     d = tempfile.mkdtemp(prefix="idash_cloud_files_")
     try:
         t0 = time.perf_counter()
-        info = filesets.write_cloud_inputs(d, seed, n_indiv, n_tags, n_targets, 5)
+        info = filesets.write_cloud_inputs(d, seed, n_indiv, n_tags, n_targets, 5, party_a=True)
         gen_s = time.perf_counter() - t0
         paths = [os.path.join(d, x) for x in ("params.bin", "model", "encrypted_data.bin", "encrypted_prediction.bin")]
         cache = os.path.join(d, "model.cache")
@@ -502,6 +506,13 @@ def section_files(seed, small=False):
         os.environ.pop("IDASH_MODEL_CACHE", None)
         out_bytes = os.path.getsize(paths[3])
         in_bytes = os.path.getsize(paths[2])
+        keys, csv = os.path.join(d, "keys.bin"), os.path.join(d, "result.csv")
+        t0 = time.perf_counter()
+        rep = gpu.encrypt_files(keys, os.path.join(d, "tags.txt"), os.path.join(d, "encrypted_data_a.bin"), seed)
+        runs["encrypt"] = {"wall_s": time.perf_counter() - t0, **rep}
+        t0 = time.perf_counter()
+        rep = gpu.decrypt_files(keys, paths[3], csv, False)
+        runs["decrypt_to_csv"] = {"wall_s": time.perf_counter() - t0, "csv_bytes": os.path.getsize(csv), **rep}
     finally:
         shutil.rmtree(d, ignore_errors=True)
     preds = info["outputs"] * n_indiv

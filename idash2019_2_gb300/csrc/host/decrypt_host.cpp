@@ -7,13 +7,19 @@
 // format and precision 6 reproduces).
 #include <cuda_runtime.h>
 
+#include <fcntl.h>
+#include <unistd.h>
+
 #include <algorithm>
+#include <cerrno>
 #include <charconv>
 #include <chrono>
 #include <cstdio>
 #include <cstring>
 #include <fstream>
+#include <memory>
 #include <thread>
+#include <vector>
 
 #include "idash_host.hpp"
 
@@ -129,29 +135,36 @@ Status write_decrypted_predictions(const DecryptedPredictions &dec, const IdashP
     }
     const uint64_t S = params.NUM_SAMPLES;
     if (S > dec.num_samples) return Status::Err(IDASH_ERR_FORMAT, "fewer decrypted samples than NUM_SAMPLES");
-    FILE *f = std::fopen(filename.c_str(), "wb");
-    if (!f) return Status::Err(IDASH_ERR_IO, "cannot open '" + filename + "' for write");
+    const int fd = ::open(filename.c_str(), O_WRONLY | O_CREAT | O_TRUNC, 0644);
+    if (fd < 0) return Status::Err(IDASH_ERR_IO, "cannot open '" + filename + "' for write");
     static const char kHeader[] = "Subject ID,target SNP,0,1,2\n";
-    bool ok = std::fwrite(kHeader, 1, sizeof(kHeader) - 1, f) == sizeof(kHeader) - 1;
+    uint64_t offset = sizeof(kHeader) - 1;
+    bool ok = ::pwrite(fd, kHeader, offset, 0) == ssize_t(offset);
 
-    // Lines in the reference's order (sample-major, positions in CSV order),
-    // formatted in chunks of samples by all threads, written in order.
+    // Lines in the reference's order (sample-major, positions in CSV order).
+    // Each round, every thread formats a chunk of samples into its own buffer
+    // (allocated once, not cleared); the chunks are then written in order.
+    // Writing them from one thread measured as fast as writing them in
+    // parallel at their offsets: the write of a 3.2 GB file is bound by the
+    // disk, not by the copy into the page cache.
     const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
     const uint64_t per_chunk = std::max<uint64_t>(1, (uint64_t(1) << 20) / std::max<uint64_t>(P, 1));  // ~1 M lines
-    std::vector<std::string> bufs(hw);
+    size_t name_max = 20;
+    for (const auto &pn : params.out_position_names) name_max = std::max(name_max, pn.second.size());
+    const size_t line_max = 20 + 1 + name_max + 1 + 3 * 16 + 4;
+    const size_t buf_bytes = size_t(per_chunk) * P * line_max;
+    std::vector<std::unique_ptr<char[]>> bufs(hw);
+    std::vector<size_t> used(hw, 0);
     for (uint64_t s0 = 0; s0 < S && ok; s0 += per_chunk * hw) {
         std::vector<std::thread> pool;
         for (unsigned t = 0; t < hw; ++t) {
             const uint64_t a = s0 + t * per_chunk, b = std::min(S, a + per_chunk);
-            bufs[t].clear();
+            used[t] = 0;
             if (a >= b) continue;
             pool.emplace_back([&, t, a, b]() {
-                std::string &out = bufs[t];
-                size_t name_max = 20;
-                for (const auto &pn : params.out_position_names) name_max = std::max(name_max, pn.second.size());
-                const size_t line_max = 20 + 1 + name_max + 1 + 3 * 16 + 4;
-                out.resize((b - a) * P * line_max);
-                char *p = &out[0], *end = p + out.size();
+                if (!bufs[t]) bufs[t].reset(new char[buf_bytes]);
+                char *const begin = bufs[t].get();
+                char *p = begin, *end = begin + buf_bytes;
                 for (uint64_t smp = a; smp < b; ++smp)
                     for (size_t q = 0; q < P; ++q) {
                         p = put_u64(p, end, smp);
@@ -169,14 +182,25 @@ Status write_decrypted_predictions(const DecryptedPredictions &dec, const IdashP
                         }
                         *p++ = '\n';
                     }
-                out.resize(size_t(p - out.data()));
+                used[t] = size_t(p - begin);
             });
         }
         for (auto &th : pool) th.join();
-        for (unsigned t = 0; t < hw && ok; ++t)
-            if (!bufs[t].empty()) ok = std::fwrite(bufs[t].data(), 1, bufs[t].size(), f) == bufs[t].size();
+        for (unsigned t = 0; t < hw && ok; ++t) {
+            size_t done = 0;
+            while (done < used[t]) {
+                const ssize_t r = ::pwrite(fd, bufs[t].get() + done, used[t] - done, off_t(offset + done));
+                if (r < 0 && errno == EINTR) continue;
+                if (r <= 0) {
+                    ok = false;
+                    break;
+                }
+                done += size_t(r);
+            }
+            offset += done;
+        }
     }
-    ok = (std::fclose(f) == 0) && ok;
+    ok = (::close(fd) == 0) && ok;
     if (!ok) return Status::Err(IDASH_ERR_IO, "short write to '" + filename + "'");
     if (n_lines) *n_lines = S * P;
     return Status::Ok();

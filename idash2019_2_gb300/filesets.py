@@ -7,6 +7,9 @@ any scale, for measuring the file pipeline:
   encrypted_data.bin  uint64 count, then records of uint32 FeatIndex, int32
                       tag 42, 2N int32 TRLWE words, double variance
                       (write_encrypted_data, eval/idash.cpp:536-556)
+  keys.bin, tags.txt  party A's inputs (optional): the secret key after the
+                      params (eval/idash.cpp:474-502) and the tag genotypes
+                      (read_plaintext_data, eval/idash.cpp:280-309)
 
 Every target takes its `neighbours` nearest tags; coefficients are seeded
 integers in [-8192, 8192).  The ciphertexts are uniformly random words (the
@@ -92,8 +95,39 @@ def write_ciphertexts(path: str, rng, n_rows: int, variance: float = 2.0 ** -50)
         f.write(rec.tobytes())
 
 
-def write_cloud_inputs(d: str, seed: int, n_indiv: int, n_tags: int, n_targets: int, neighbours: int = 5) -> dict:
-    """params.bin, model/ and encrypted_data.bin for one cloud step in `d`."""
+def write_keys(path: str, params_path: str, rng) -> np.ndarray:
+    """keys.bin as the reference's keygen writes it (eval/idash.cpp:474-502):
+    params.bin's bytes, then the TRLWE key record: int32 tag 52, N, k = 1,
+    double alpha_min and alpha_max, N binary int32 coefficients."""
+    key = rng.integers(0, 2, size=N).astype("<i4")
+    with open(params_path, "rb") as f:
+        params = f.read()
+    with open(path, "wb") as f:
+        f.write(params)
+        f.write(np.array([52, N, 1], dtype="<i4").tobytes())
+        f.write(np.array([2.0 ** -25, 2.0 ** -10], dtype="<f8").tobytes())
+        f.write(key.tobytes())
+    return key
+
+
+def write_challenge(path: str, rng, tag_pos, n_indiv: int, missing: float = 0.05) -> None:
+    """The tag genotypes (read_plaintext_data, eval/idash.cpp:280-309): per tag
+    "22 <pos> <pos+1> rs<pos> <g_0> ... <g_{n-1}>", '.' for a missing value."""
+    geno = rng.integers(0, 3, size=(len(tag_pos), n_indiv)).astype(np.uint8) + ord("0")
+    geno[rng.random(size=geno.shape) < missing] = ord(".")
+    cells = np.full((len(tag_pos), 2 * n_indiv), ord(" "), dtype=np.uint8)
+    cells[:, 0::2] = geno
+    cells[:, -1] = ord("\n")
+    with open(path, "wb") as f:
+        for i, pos in enumerate(tag_pos.tolist()):
+            f.write(f"22 {pos} {pos + 1} rs{pos} ".encode())
+            f.write(cells[i].tobytes())
+
+
+def write_cloud_inputs(d: str, seed: int, n_indiv: int, n_tags: int, n_targets: int, neighbours: int = 5,
+                       party_a: bool = False) -> dict:
+    """params.bin, model/ and encrypted_data.bin for one cloud step in `d`;
+    with party_a, also keys.bin and the tag genotypes file tags.txt."""
     os.makedirs(d, exist_ok=True)
     rng = np.random.default_rng(seed)
     tag_pos, tgt = _positions(rng, n_tags, n_targets)
@@ -103,4 +137,7 @@ def write_cloud_inputs(d: str, seed: int, n_indiv: int, n_tags: int, n_targets: 
     R = N // n_indiv
     n_rows = (3 * n_tags + R - 1) // R
     write_ciphertexts(os.path.join(d, "encrypted_data.bin"), rng, n_rows)
+    if party_a:
+        write_keys(os.path.join(d, "keys.bin"), os.path.join(d, "params.bin"), rng)
+        write_challenge(os.path.join(d, "tags.txt"), rng, tag_pos, n_indiv)
     return {"outputs": 3 * n_targets, "terms": terms, "in_records": n_rows}
