@@ -117,14 +117,34 @@ __global__ void k_synth_trlwe(uint64_t seed, uint32_t N, uint32_t num_samples, u
     }
 }
 
+// Hash of one output word keyed by its index: for each index a bijection of
+// the word (odd multiplies and xor-shifts), all in 32-bit arithmetic.
+__host__ __device__ __forceinline__ uint32_t word_hash(uint64_t index, uint32_t w) {
+    uint32_t x = w * 0x9E3779B1u + uint32_t(index) * 0x85EBCA77u + uint32_t(index >> 32) * 0xC2B2AE3Du;
+    x ^= x >> 15;
+    x *= 0x2C1B3C6Du;
+    x ^= x >> 12;
+    return x;
+}
+
 // Order-independent digest of a request's output words: the sum mod 2^64 of
-// mix64(index << 32 | word) over every word, accumulated into *digest.
+// word_hash(global index, word) over every word, accumulated into *digest.
+// The first pass over a 1 GB output hashed with 64-bit multiplies cost as
+// much as scoring it; 16-byte loads and 32-bit arithmetic stream it.
 __global__ void k_digest(const uint32_t *words, uint64_t n_words, uint64_t index_base,
                          unsigned long long *digest) {
     uint64_t acc = 0;
-    for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n_words;
-         i += uint64_t(gridDim.x) * blockDim.x)
-        acc += mix64(((index_base + i) << 32) | words[i]);
+    const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
+    const uint64_t first = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    // quads when the words start 16-byte aligned, then the tail one by one
+    const uint64_t n4 = (reinterpret_cast<uintptr_t>(words) & 15u) == 0 ? n_words / 4 : 0;
+    const uint4 *w4 = reinterpret_cast<const uint4 *>(words);
+    for (uint64_t q = first; q < n4; q += stride) {
+        const uint4 v = w4[q];
+        const uint64_t i = index_base + 4 * q;
+        acc += uint64_t(word_hash(i, v.x)) + word_hash(i + 1, v.y) + word_hash(i + 2, v.z) + word_hash(i + 3, v.w);
+    }
+    for (uint64_t i = 4 * n4 + first; i < n_words; i += stride) acc += word_hash(index_base + i, words[i]);
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xFFFFFFFFu, acc, off);
     if ((threadIdx.x & 31) == 0) atomicAdd(digest, (unsigned long long)acc);
@@ -177,7 +197,7 @@ cudaError_t digest_words(const uint32_t *words, uint64_t n_words, uint64_t index
 
 uint64_t digest_host(const uint32_t *words, uint64_t n_words, uint64_t index_base) {
     uint64_t acc = 0;
-    for (uint64_t i = 0; i < n_words; ++i) acc += mix64(((index_base + i) << 32) | words[i]);
+    for (uint64_t i = 0; i < n_words; ++i) acc += word_hash(index_base + i, words[i]);
     return acc;
 }
 
