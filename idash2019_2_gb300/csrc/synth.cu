@@ -156,11 +156,11 @@ __global__ void k_digest(const uint32_t *words, uint64_t n_words, uint64_t index
 __global__ void k_fill_uniform(uint64_t seed, uint64_t row_begin, uint64_t n_rows, uint32_t row_words,
                                uint8_t *base, uint64_t stride) {
     const uint64_t key = stream_key(seed, 7);
-    const uint64_t total = n_rows * row_words;
-    for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < total;
-         i += uint64_t(gridDim.x) * blockDim.x) {
-        const uint64_t r = i / row_words, j = i % row_words;
-        reinterpret_cast<uint32_t *>(base + r * stride)[j] = hash32k(key, (row_begin + r) * row_words + j);
+    // a row per block (grid-stride), its words across the threads: no division
+    for (uint64_t r = blockIdx.x; r < n_rows; r += gridDim.x) {
+        uint32_t *out = reinterpret_cast<uint32_t *>(base + r * stride);
+        const uint64_t w0 = (row_begin + r) * row_words;
+        for (uint32_t j = threadIdx.x; j < row_words; j += blockDim.x) out[j] = hash32k(key, w0 + j);
     }
 }
 
@@ -169,8 +169,7 @@ __global__ void k_fill_uniform(uint64_t seed, uint64_t row_begin, uint64_t n_row
 cudaError_t fill_uniform_rows(uint64_t seed, uint64_t row_begin, uint64_t n_rows, uint32_t row_words, uint8_t *d_out,
                               uint64_t row_stride, int sm_count, cudaStream_t s) {
     if (n_rows == 0) return cudaSuccess;
-    const uint64_t want = (n_rows * row_words + 255) / 256;
-    const uint32_t blocks = uint32_t(std::min<uint64_t>(want, uint64_t(sm_count) * 16));
+    const uint32_t blocks = uint32_t(std::min<uint64_t>(n_rows, uint64_t(sm_count) * 16));
     k_fill_uniform<<<blocks, 256, 0, s>>>(seed, row_begin, n_rows, row_words, d_out, row_stride);
     return cudaGetLastError();
 }
