@@ -142,6 +142,19 @@ def dist_env():
     return rank, world, local
 
 
+def max_over_ranks(x: float) -> float:
+    """The largest x over the process group (x itself without one): a
+    multi-GPU timing is the slowest rank's.  NCCL reduces on the device, gloo
+    on the host."""
+    import torch
+    import torch.distributed as dist
+    if not dist.is_available() or not dist.is_initialized() or dist.get_world_size() == 1:
+        return x
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if dist.get_backend() == "nccl" else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def cpu_baseline(model_csr, rows, spec, min_seconds=10.0, max_reps=1000):
     """The oracle's restatement of the reference loop (OpenMP over outputs,
     eval/idash.cpp:779-842) on all host cores, full workload per rep."""
@@ -605,11 +618,7 @@ def run_ours(args):
     ctx.sync()
     torch.cuda.synchronize()
     launches = ctx.stats()["kernel_launches"] - launches0
-    ms = e0.elapsed_time(e1)
-    if world > 1:
-        tt = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        ms = float(tt.item())
+    ms = max_over_ranks(e0.elapsed_time(e1))
     time.sleep(0.25)
     clocks = sampler.summary(t0, t1)
     sampler.stop()
@@ -640,11 +649,7 @@ def run_ours(args):
     te0 = time.perf_counter()
     for _ in range(e2e_steps):
         model.score_host(h_in.ptr, lay, spec["n_rows"], h_out.ptr, lay)
-    te = time.perf_counter() - te0
-    if world > 1:
-        tt = torch.tensor([te], device="cuda")
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        te = float(tt.item())
+    te = max_over_ranks(time.perf_counter() - te0)
     st1 = ctx.stats()
     e2e = {"value": preds_per_step * world * e2e_steps / te, "unit": UNIT,
            "h2d_bytes_per_step": (st1["h2d_bytes"] - st0["h2d_bytes"]) // e2e_steps,
