@@ -9,6 +9,7 @@
 // encryptions of zero plus the one-hot messages, in one kernel launch.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -16,6 +17,8 @@
 #include <fstream>
 #include <random>
 #include <sstream>
+#include <thread>
+#include <vector>
 
 #include "idash_host.hpp"
 
@@ -39,30 +42,59 @@ Status read_plaintext_data(PlaintextData &plain, const IdashParams &params, cons
     std::ifstream challenge(filename);
     if (!challenge) return Status::Err(IDASH_ERR_IO, "cannot open challenge file '" + filename + "'");
     plain = PlaintextData();
+    // The lines the reference reads (at most NUM_INPUT_POSITIONS), each parsed
+    // as the reference parses it, token by token with an istringstream, on
+    // host threads; then inserted into the map in file order, so that its
+    // iteration order is the reference's.
+    std::vector<std::string> lines;
     std::string line;
-    uint64_t read = 0;
-    // the reference's parse, token by token (an istringstream per line)
-    for (std::getline(challenge, line); challenge; std::getline(challenge, line)) {
-        std::istringstream iss(line);
+    for (std::getline(challenge, line); challenge && lines.size() < params.NUM_INPUT_POSITIONS;
+         std::getline(challenge, line))
+        lines.push_back(std::move(line));
+    struct Parsed {
+        uint64_t position = 0;
+        std::vector<int8_t> values;
+        Status st = Status::Ok();
+    };
+    std::vector<Parsed> parsed(lines.size());
+    auto parse = [&](size_t i) {
+        Parsed &out = parsed[i];
+        std::istringstream iss(lines[i]);
         int chrom = 0;  // must be 22
-        uint64_t position = 0, position2 = 0;
+        uint64_t position2 = 0;
         std::string name;
         iss >> chrom;
-        if (chrom != 22)
-            return Status::Err(IDASH_ERR_FORMAT, filename + ": line " + std::to_string(read + 1) +
-                                                     " does not start with 22");
-        iss >> position >> position2 >> name;
-        if (!iss) return Status::Err(IDASH_ERR_FORMAT, filename + ": line " + std::to_string(read + 1) + " is short");
-        std::vector<int8_t> &v = plain.data[position];
-        v.resize(params.NUM_SAMPLES);
+        if (chrom != 22) {
+            out.st = Status::Err(IDASH_ERR_FORMAT, filename + ": line " + std::to_string(i + 1) +
+                                                       " does not start with 22");
+            return;
+        }
+        iss >> out.position >> position2 >> name;
+        if (!iss) {
+            out.st = Status::Err(IDASH_ERR_FORMAT, filename + ": line " + std::to_string(i + 1) + " is short");
+            return;
+        }
+        out.values.resize(params.NUM_SAMPLES);
         std::string snp;
         for (uint32_t s = 0; s < params.NUM_SAMPLES; ++s) {
             iss >> snp;  // keeps the previous token when the line runs out, as the reference's loop does
-            v[s] = (snp == "0" || snp == "1" || snp == "2") ? int8_t(snp[0] - '0') : int8_t(-1);
+            out.values[s] = (snp == "0" || snp == "1" || snp == "2") ? int8_t(snp[0] - '0') : int8_t(-1);
         }
-        if (++read >= params.NUM_INPUT_POSITIONS) break;
+    };
+    const size_t n_threads =
+        std::max<size_t>(1, std::min<size_t>({16, std::thread::hardware_concurrency(), lines.size() / 64 + 1}));
+    std::vector<std::thread> threads;
+    for (size_t t = 1; t < n_threads; ++t)
+        threads.emplace_back([&, t] {
+            for (size_t i = lines.size() * t / n_threads; i < lines.size() * (t + 1) / n_threads; ++i) parse(i);
+        });
+    for (size_t i = 0; i < lines.size() / n_threads; ++i) parse(i);
+    for (auto &th : threads) th.join();
+    for (Parsed &p : parsed) {
+        if (!p.st.ok()) return p.st;  // the first failure in file order
+        plain.data[p.position] = std::move(p.values);
     }
-    if (read != params.NUM_INPUT_POSITIONS)
+    if (parsed.size() != params.NUM_INPUT_POSITIONS)
         return Status::Err(IDASH_ERR_FORMAT, filename + ": missing positions in plaintext file");
     return Status::Ok();
 }
