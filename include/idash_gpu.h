@@ -192,7 +192,8 @@ typedef struct {
     double admit_s;        /* admission, seconds after the start (host clock) */
     double done_s;         /* device completion, seconds after the start (CUDA events) */
     uint64_t device_bytes; /* HBM the request held while in flight */
-    uint64_t digest;       /* sum mod 2^64 of mix64(index << 32 | word) over its output words */
+    uint64_t digest;       /* sum mod 2^64 over its output words of a 32-bit hash of (index, word);
+                              idash_digest_host restates it */
 } idash_request_result;
 typedef struct {
     uint64_t hbm_budget;   /* device bytes the in-flight requests may hold together */
