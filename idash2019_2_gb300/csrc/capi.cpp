@@ -958,9 +958,15 @@ idash_status idash_model_input_rows(const idash_model *m, uint64_t out_begin, ui
     return IDASH_OK;
 }
 
-idash_status idash_score_trlwe_range(idash_model *m, uint64_t out_begin, uint64_t out_end, uint32_t num_samples,
-                                     const void *d_in, const idash_row_layout *il, uint64_t in_row_base,
-                                     uint64_t n_in_rows, void *d_out, const idash_row_layout *ol, void *stream) {
+}  // extern "C"
+
+namespace idash {
+
+idash_status score_trlwe_range(idash_model *m, uint64_t out_begin, uint64_t out_end, uint32_t num_samples,
+                               const void *d_in, const idash_row_layout *il, uint64_t in_row_base, uint64_t n_in_rows,
+                               void *d_out, const idash_row_layout *ol, void *stream, uint64_t *digest,
+                               uint64_t digest_base, bool *fused) {
+    if (fused) *fused = false;
     if (!m || !d_in || !d_out || !il || !ol) return IDASH_ERR_INVALID_ARGUMENT;
     idash_ctx *ctx = m->ctx;
     if (m->form != Form::kTrlwe) return ctx->fail(IDASH_ERR_STATE, "model is not a TRLWE model");
@@ -981,6 +987,12 @@ idash_status idash_score_trlwe_range(idash_model *m, uint64_t out_begin, uint64_
     cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
     const uint8_t *in = static_cast<const uint8_t *>(d_in);
     uint8_t *out = static_cast<uint8_t *>(d_out);
+    // The digest rides in the scoring kernel when every output word is
+    // written once, by one launch, into dense rows (word c of row r is word
+    // r * 2N + c of the output image).
+    const bool fuse = digest && n_phases(m) == 1 && ol->payload_offset == 0 && ol->row_stride == payload &&
+                      ol->variance_offset < 0 && ol->header_offset < 0 && digest_base % 4 == 0 &&
+                      digest_fusable(m->kind, m->slice_words, m->group_size);
     s = launch_phases(m, out_begin, out_end, st, [&](uint32_t lo, uint32_t hi) {
         ScoreArgs a = make_args(m, in + il->payload_offset, il->row_stride, out + ol->payload_offset, ol->row_stride,
                                 row_words_of(m, 0), lo, hi, out_begin, out_end, out_begin);
@@ -988,9 +1000,14 @@ idash_status idash_score_trlwe_range(idash_model *m, uint64_t out_begin, uint64_
         a.row_base = uint32_t(in_row_base);
         a.n_rows = uint32_t(n_in_rows);
         if (num_samples) a.num_samples = num_samples;
+        if (fuse) {
+            a.digest = reinterpret_cast<unsigned long long *>(digest);
+            a.digest_base = digest_base;
+        }
         return a;
     });
     if (s != IDASH_OK) return s;
+    if (fused) *fused = fuse;
     FinalizeArgs f{};
     f.var_ptr = m->d_var_ptr;
     f.var_row = m->d_var_row;
@@ -1010,6 +1027,17 @@ idash_status idash_score_trlwe_range(idash_model *m, uint64_t out_begin, uint64_
     f.out_hdr_off = ol->header_offset;
     f.tag = m->tp.record_tag;
     return ctx->check_cuda(launch_finalize(f, st), "finalize launch");
+}
+
+}  // namespace idash
+
+extern "C" {
+
+idash_status idash_score_trlwe_range(idash_model *m, uint64_t out_begin, uint64_t out_end, uint32_t num_samples,
+                                     const void *d_in, const idash_row_layout *il, uint64_t in_row_base,
+                                     uint64_t n_in_rows, void *d_out, const idash_row_layout *ol, void *stream) {
+    return score_trlwe_range(m, out_begin, out_end, num_samples, d_in, il, in_row_base, n_in_rows, d_out, ol, stream,
+                             nullptr, 0, nullptr);
 }
 
 idash_status idash_score_lwe_device(idash_model *m, uint32_t n_indiv, const int32_t *d_in, uint64_t in_row_stride,

@@ -23,10 +23,18 @@ cudaError_t synth_trlwe_rows(uint64_t seed, const idash_trlwe_params &p, uint64_
 cudaError_t fill_uniform_rows(uint64_t seed, uint64_t row_begin, uint64_t n_rows, uint32_t row_words, uint8_t *d_out,
                               uint64_t row_stride, int sm_count, cudaStream_t s);
 // Adds to *d_digest the order-independent digest of n_words output words
-// (sum mod 2^64 of mix64(index << 32 | word), index = index_base + i).
+// (sum mod 2^64 of word_hash(index_base + i, word i)).
 cudaError_t digest_words(const uint32_t *words, uint64_t n_words, uint64_t index_base, uint64_t *d_digest,
                          int sm_count, cudaStream_t s);
 uint64_t digest_host(const uint32_t *words, uint64_t n_words, uint64_t index_base);
+// idash_score_trlwe_range that can also take the digest of the outputs it
+// writes, added to *digest (the one of digest_words over the output image,
+// with index_base = digest_base).  *fused tells whether it did; when not,
+// the caller digests the outputs itself.
+idash_status score_trlwe_range(idash_model *m, uint64_t out_begin, uint64_t out_end, uint32_t num_samples,
+                               const void *d_in, const idash_row_layout *il, uint64_t in_row_base, uint64_t n_in_rows,
+                               void *d_out, const idash_row_layout *ol, void *stream, uint64_t *digest,
+                               uint64_t digest_base, bool *fused);
 
 // The nonzero coefficients of an integer key polynomial (positions, values),
 // staged on the device for launches on `s` and released stream-ordered after

@@ -19,6 +19,29 @@ __host__ __device__ __forceinline__ uint64_t mix64(uint64_t z) {
     return z ^ (z >> 31);
 }
 
+// Hash of one output word keyed by its index: for each index a bijection of
+// the word (an added key, then xor-shifts around an odd multiply), all in
+// 32-bit arithmetic.  The serving digest is the sum mod 2^64 of word_hash over
+// a request's output words.  The key of index i + d, when the low word of i
+// does not wrap on adding d, is hash_index_key(i) + d * kHashLo: keys along a
+// row follow by addition.
+constexpr uint32_t kHashLo = 0x85EBCA77u, kHashHi = 0xC2B2AE3Du;
+
+__host__ __device__ __forceinline__ uint32_t hash_index_key(uint64_t index) {
+    return uint32_t(index) * kHashLo + uint32_t(index >> 32) * kHashHi;
+}
+
+__host__ __device__ __forceinline__ uint32_t hash_finish(uint32_t x) {
+    x ^= x >> 15;
+    x *= 0x2C1B3C6Du;
+    x ^= x >> 12;
+    return x;
+}
+
+__host__ __device__ __forceinline__ uint32_t word_hash(uint64_t index, uint32_t w) {
+    return hash_finish(w + hash_index_key(index));
+}
+
 // ~1 s at the GB300's 2.07 GHz maximum SM clock.
 constexpr long long kWaitLimitCycles = 2000000000ll;
 

@@ -144,6 +144,35 @@ __device__ __forceinline__ void write_outputs(const ScoreArgs &a, const PlanGrou
     }
 }
 
+// The fused digest: adds word_hash(index, word) of every word write_outputs
+// stored (acc holds the stored values) to `dig`.  When the low word of the
+// slice's first index leaves room for W more, every key of the slice is that
+// index's key plus (column offset) * kHashLo.
+template <int W, int G, int Q, int TEAM>
+__device__ __forceinline__ void digest_outputs(const ScoreArgs &a, const PlanGroup &gr,
+                                               const uint32_t (&acc)[G][4 * Q], uint32_t c0, uint32_t lane,
+                                               uint32_t valid, uint64_t &dig) {
+    const uint64_t row_words = a.out_stride / 4;
+#pragma unroll
+    for (int m = 0; m < G; ++m) {
+        const uint32_t o = gr.out[m];
+        if (o == kNoOutput || o < a.out_lo || o >= a.out_hi) continue;
+        const uint64_t r = a.out_row_map ? uint64_t(a.out_row_map[o]) : uint64_t(o) - a.out_row_base;
+        const uint64_t base = a.digest_base + r * row_words + c0;
+        const bool flat = uint32_t(base) <= 0xFFFFFFFFu - uint32_t(W);
+        const uint32_t key_lane = hash_index_key(base) + 4 * lane * kHashLo;
+#pragma unroll
+        for (int k = 0; k < Q; ++k) {
+            const uint32_t q = 4 * lane + 4 * k * TEAM;
+            const uint32_t key = flat ? key_lane + uint32_t(4 * k * TEAM) * kHashLo : hash_index_key(base + q);
+#pragma unroll
+            for (int e = 0; e < 4; ++e)
+                if (q + 4 <= valid || q + e < valid)
+                    dig += hash_finish(acc[m][4 * k + e] + key + uint32_t(e) * kHashLo);
+        }
+    }
+}
+
 template <int G, int Q>
 __device__ __forceinline__ void mac(uint32_t (&acc)[G][4 * Q], const PlanTerm &tm, const uint4 (&x)[Q]) {
     const uint32_t c[3] = {uint32_t(tm.c0), uint32_t(tm.c1), uint32_t(tm.c2)};
@@ -488,7 +517,10 @@ static_assert(2 * kWsMaxStages * 8 + kWsMaxStages * sizeof(WsStageHeader) <= kWs
 // counter, so uneven groups balance across warps; a warp that runs out of
 // units arrives on `empty[s]` and moves on to the next stage.  No CTA-wide
 // barrier: the next stages' copies overlap this stage's arithmetic.
-template <int W, int G, int Q>
+//
+// DIG: the instance that also takes the serving digest of what it writes
+// (ScoreArgs::digest); one atomic add per consumer warp at the end.
+template <int W, int G, int Q, bool DIG>
 __global__ void __launch_bounds__(kWsThreads, 1) k_score_ws(const ScoreArgs a) {
     constexpr int TEAM = W / (4 * Q);
     constexpr int PARTS = TEAM / 32;  // warps per group-slice
@@ -577,11 +609,19 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_score_ws(const ScoreArgs a) {
     }
 
     // --------------------------------------------------------------- consumers
+    uint64_t dig = 0;  // DIG only
     for (uint32_t it = 0;; ++it) {
         const uint32_t s = it % n_stages, round = it / n_stages;
         if (!mbar_wait_bounded(&full[s], round & 1u, a.err)) return;
         const uint32_t tile = hdr[s].tile;
-        if (tile >= a.n_tiles) return;
+        if (tile >= a.n_tiles) {
+            if (DIG) {
+#pragma unroll
+                for (int off = 16; off > 0; off >>= 1) dig += __shfl_xor_sync(0xFFFFFFFFu, dig, off);
+                if (lane == 0 && dig) atomicAdd(a.digest, (unsigned long long)dig);
+            }
+            return;
+        }
         const PlanBlock blk = hdr[s].blk;
         const uint32_t c0 = (tile / a.n_blocks) * W;
         const uint32_t valid = min(uint32_t(W), a.row_words - c0);
@@ -612,6 +652,7 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_score_ws(const ScoreArgs a) {
             accumulate_group<W, G, Q, TEAM>(acc, gr, terms_s + gr.term_begin, win_of(s) + 4 * tlane, bias_mask,
                                             zero_mask);
             write_outputs<G, Q, TEAM>(a, gr, acc, c0, tlane, valid, zero_mask);
+            if (DIG) digest_outputs<W, G, Q, TEAM>(a, gr, acc, c0, tlane, valid, dig);
             u = __shfl_sync(0xFFFFFFFFu, u_next, 0);
         }
         __syncwarp();
@@ -726,11 +767,11 @@ KernelFn pick(KernelKind kind, uint32_t w) {
             break;
         case KernelKind::kWs:
             switch (w) {
-                case 128: return k_score_ws<128, G, 1>;
-                case 256: return k_score_ws<256, G, 2>;
-                case 512: return k_score_ws<512, G, 4>;
-                case 1024: return k_score_ws<1024, G, 4>;
-                case 2048: return k_score_ws<2048, G, 4>;
+                case 128: return k_score_ws<128, G, 1, false>;
+                case 256: return k_score_ws<256, G, 2, false>;
+                case 512: return k_score_ws<512, G, 4, false>;
+                case 1024: return k_score_ws<1024, G, 4, false>;
+                case 2048: return k_score_ws<2048, G, 4, false>;
             }
             break;
         case KernelKind::kDirect:
@@ -750,11 +791,26 @@ KernelFn pick_kernel(KernelKind kind, uint32_t w, uint32_t g) {
     return g == 1 ? pick<1>(kind, w) : g == 3 ? pick<3>(kind, w) : nullptr;
 }
 
+// The fused-digest instances: the warp-specialised kernel, groups of 3.
+KernelFn pick_digest(KernelKind kind, uint32_t w, uint32_t g) {
+    if (kind != KernelKind::kWs || g != 3) return nullptr;
+    switch (w) {
+        case 128: return k_score_ws<128, 3, 1, true>;
+        case 256: return k_score_ws<256, 3, 2, true>;
+        case 512: return k_score_ws<512, 3, 4, true>;
+        case 1024: return k_score_ws<1024, 3, 4, true>;
+        case 2048: return k_score_ws<2048, 3, 4, true>;
+    }
+    return nullptr;
+}
+
 uint32_t threads_of(KernelKind kind) {
     return kind == KernelKind::kPipe ? kPipeThreads : kind == KernelKind::kWs ? kWsThreads : kThreads;
 }
 
 }  // namespace
+
+bool digest_fusable(KernelKind kind, uint32_t w, uint32_t g) { return pick_digest(kind, w, g) != nullptr; }
 
 bool slice_supported(uint32_t w) { return w == 128 || w == 256 || w == 512 || w == 1024 || w == 2048; }
 
@@ -778,9 +834,11 @@ cudaError_t configure_window_kernels(size_t max_smem) {
     for (KernelKind kind : {KernelKind::kWindow, KernelKind::kPipe, KernelKind::kWs})
         for (uint32_t w : {128u, 256u, 512u, 1024u, 2048u})
             for (uint32_t g : {1u, 3u}) {
-                cudaError_t e = cudaFuncSetAttribute(pick_kernel(kind, w, g),
-                                                     cudaFuncAttributeMaxDynamicSharedMemorySize, int(max_smem));
-                if (e != cudaSuccess) return e;
+                for (KernelFn fn : {pick_kernel(kind, w, g), pick_digest(kind, w, g)}) {
+                    if (!fn) continue;
+                    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(max_smem));
+                    if (e != cudaSuccess) return e;
+                }
             }
     return cudaSuccess;
 }
@@ -796,8 +854,8 @@ int resident_ctas_per_sm(KernelKind kind, uint32_t slice_words, uint32_t group_s
 
 cudaError_t launch_score(KernelKind kind, uint32_t slice_words, uint32_t group_size, const ScoreArgs &a,
                          uint32_t ctas, cudaStream_t stream) {
-    KernelFn fn = pick_kernel(kind, slice_words, group_size);
-    if (!fn) return cudaErrorInvalidValue;
+    KernelFn fn = a.digest ? pick_digest(kind, slice_words, group_size) : pick_kernel(kind, slice_words, group_size);
+    if (!fn || (a.digest && a.accumulate)) return cudaErrorInvalidValue;
     if (a.n_tiles == 0) return cudaSuccess;
     if (kind == KernelKind::kDirect) {
         fn<<<a.n_tiles, kThreads, 0, stream>>>(a);

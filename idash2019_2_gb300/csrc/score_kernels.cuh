@@ -37,6 +37,11 @@ struct ScoreArgs {
     uint32_t accumulate;          // 1: add to the outputs (later parts of split groups)
     uint32_t *tile_counter;       // persistent kernel: next tile (zeroed before launch)
     uint32_t *err;                // device error word
+    // k_score_ws with the fused digest only (null otherwise): the sum mod 2^64
+    // of word_hash(digest_base + r * out_stride / 4 + c, word) over the words
+    // written, row r and column c, is added to *digest.
+    unsigned long long *digest;
+    uint64_t digest_base;         // a multiple of 4
 };
 
 // kWindow: persistent, 256 threads, one shared-memory buffer, 1-2 CTAs/SM.
@@ -62,6 +67,9 @@ size_t kernel_smem_bytes(KernelKind kind, uint32_t slice_words, uint32_t max_slo
 inline size_t window_smem_bytes(uint32_t slice_words, uint32_t max_slots, uint32_t max_terms, uint32_t max_groups) {
     return kernel_smem_bytes(KernelKind::kWindow, slice_words, max_slots, max_terms, max_groups);
 }
+
+// Whether the kernel kind can take the fused digest (ScoreArgs::digest).
+bool digest_fusable(KernelKind kind, uint32_t slice_words, uint32_t group_size);
 
 // Launches one scoring kernel.  `ctas` is the persistent grid size (window
 // and pipe kernels) and is ignored by the direct kernel (one CTA per tile).

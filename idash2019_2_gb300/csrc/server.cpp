@@ -13,7 +13,9 @@
 // and the request's device memory fits the HBM budget (first fit in one arena
 // allocated at start).  Admitted requests run concurrently, one stream each:
 // ciphertext synthesis (standing in for the request's payload), range
-// scoring, and an order-independent digest of the outputs.  Memory returns to
+// scoring, and an order-independent digest of the outputs (taken by the
+// scoring kernel as it stores them when the model's kernel can, else by a
+// pass over the outputs).  Memory returns to
 // the arena when a request completes.  Completion times come from CUDA events.
 #include <algorithm>
 #include <chrono>
@@ -213,13 +215,15 @@ extern "C" idash_status idash_serve_trlwe(idash_model *m, const idash_serve_conf
                                                        sh.row_end - sh.row_begin, 2 * N, in_b, row_bytes,
                                                        ctx->sm_count, s.stream),
                                      "request ciphertexts");
+                const uint64_t index_base = uint64_t(b) * (sh.out_bytes_per_block / 4);
+                bool fused = false;
                 if (st == IDASH_OK)
-                    st = idash_score_trlwe_range(m, sh.out_begin, sh.out_end, ns, in_b, &dense, sh.row_begin,
-                                                 sh.row_end - sh.row_begin, out_b, &dense, s.stream);
-                if (st == IDASH_OK)
+                    st = score_trlwe_range(m, sh.out_begin, sh.out_end, ns, in_b, &dense, sh.row_begin,
+                                           sh.row_end - sh.row_begin, out_b, &dense, s.stream, d_digest + i,
+                                           index_base, &fused);
+                if (st == IDASH_OK && !fused)
                     st = ctx->check_cuda(digest_words(reinterpret_cast<const uint32_t *>(out_b),
-                                                      sh.out_bytes_per_block / 4,
-                                                      uint64_t(b) * (sh.out_bytes_per_block / 4), d_digest + i,
+                                                      sh.out_bytes_per_block / 4, index_base, d_digest + i,
                                                       ctx->sm_count, s.stream),
                                          "digest");
             }

@@ -117,20 +117,11 @@ __global__ void k_synth_trlwe(uint64_t seed, uint32_t N, uint32_t num_samples, u
     }
 }
 
-// Hash of one output word keyed by its index: for each index a bijection of
-// the word (odd multiplies and xor-shifts), all in 32-bit arithmetic.
-__host__ __device__ __forceinline__ uint32_t word_hash(uint64_t index, uint32_t w) {
-    uint32_t x = w * 0x9E3779B1u + uint32_t(index) * 0x85EBCA77u + uint32_t(index >> 32) * 0xC2B2AE3Du;
-    x ^= x >> 15;
-    x *= 0x2C1B3C6Du;
-    x ^= x >> 12;
-    return x;
-}
-
 // Order-independent digest of a request's output words: the sum mod 2^64 of
 // word_hash(global index, word) over every word, accumulated into *digest.
-// The first pass over a 1 GB output hashed with 64-bit multiplies cost as
-// much as scoring it; 16-byte loads and 32-bit arithmetic stream it.
+// A pass over the outputs, for scoring kernels that do not take the digest
+// as they store (the warp-specialised one does).  16-byte loads and 32-bit
+// arithmetic stream it at close to the HBM copy rate.
 __global__ void k_digest(const uint32_t *words, uint64_t n_words, uint64_t index_base,
                          unsigned long long *digest) {
     uint64_t acc = 0;

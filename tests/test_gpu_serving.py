@@ -46,6 +46,34 @@ def test_digests_restate_on_the_host(served):
         assert d == res[i]["digest"]
 
 
+@pytest.mark.parametrize("slice_words", [128, 512])
+def test_fused_digest_of_the_warp_specialised_kernel(served, slice_words):
+    """With the warp-specialised kernel the scoring kernel takes the digest as
+    it stores the outputs (no separate pass).  Its digests equal the host
+    restatement over the outputs and the autotuned model's digests, and the
+    outputs are the same."""
+    ctx, w, m, reqs, res, outs = served
+    import ctypes as C
+    pick = (0, 2, 5)  # request 2 spans several TRLWE blocks (over 1,024 individuals)
+    ctx.set_option("kernel", 4)
+    ctx.set_option("slice_words", slice_words)
+    try:
+        m2 = gpu.TrlweModel(ctx, w.model, 900, 1024, 1, 1024)
+        assert m2.info()["kernel"] == 3
+        res2, outs2 = m2.serve([dict(reqs[i], arrival_s=0.0) for i in pick], hbm_budget=2 << 30, max_inflight=2,
+                               keep_outputs=True)
+        m2.free()
+    finally:
+        ctx.set_option("kernel", 0)
+        ctx.set_option("slice_words", 0)
+    assert sum(reqs[i]["n_indiv"] > 1024 for i in pick) >= 1
+    for j, i in enumerate(pick):
+        np.testing.assert_array_equal(outs2[j], outs[i])
+        words = np.ascontiguousarray(outs2[j]).view(np.uint32).ravel()
+        d = ctx.lib.idash_digest_host(words.ctypes.data_as(C.POINTER(C.c_uint32)), words.size, 0)
+        assert d == res2[j]["digest"] == res[i]["digest"]
+
+
 def test_the_mix_overlaps_requests(served):
     ctx, w, m, reqs, res, outs = served
     spans = sorted((r["admit_s"], r["done_s"]) for r in res)
