@@ -273,24 +273,39 @@ idash_status enqueue_trlwe(idash_model *m, const void *d_in, const idash_row_lay
 
 bool same_layout(const idash_row_layout &x, const idash_row_layout &y) { return std::memcmp(&x, &y, sizeof(x)) == 0; }
 
+// Orders `waiter` after the work enqueued so far on `done` (through the
+// context's event number `ev`).
+idash_status stream_after(idash_ctx *ctx, cudaStream_t waiter, cudaStream_t done, size_t ev) {
+    cudaEvent_t e = ctx->event(ev);
+    if (!e) return ctx->fail(IDASH_ERR_CUDA, "cudaEventCreate failed");
+    idash_status s = ctx->check_cuda(cudaEventRecord(e, done), "cudaEventRecord");
+    if (s == IDASH_OK) s = ctx->check_cuda(cudaStreamWaitEvent(waiter, e, 0), "cudaStreamWaitEvent");
+    return s;
+}
+
+// Milliseconds per run of `reps` runs of `run` on `s` between two events;
+// -1 when a run, an event or the stream fails.
+template <class F>
+float time_runs(cudaEvent_t e0, cudaEvent_t e1, cudaStream_t s, int reps, F run) {
+    if (!e0 || !e1 || run() != IDASH_OK) return -1.f;  // the first run warms up
+    if (cudaEventRecord(e0, s) != cudaSuccess) return -1.f;
+    for (int r = 0; r < reps; ++r)
+        if (run() != IDASH_OK) return -1.f;
+    if (cudaEventRecord(e1, s) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess) return -1.f;
+    float ms = 0;
+    if (cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) return -1.f;
+    return ms / reps;
+}
+
 // Times `reps` runs of the current plan on the caller's buffers.
 float time_candidate(idash_model *m, const void *d_in, const idash_row_layout *il, void *d_out,
                      const idash_row_layout *ol, cudaStream_t s, int reps) {
-    cudaEvent_t e0 = m->ctx->event(0), e1 = m->ctx->event(1);
-    if (enqueue_trlwe(m, d_in, il, d_out, ol, s) != IDASH_OK) return -1.f;  // warm-up
-    cudaEventRecord(e0, s);
-    for (int r = 0; r < reps; ++r)
-        if (enqueue_trlwe(m, d_in, il, d_out, ol, s) != IDASH_OK) return -1.f;
-    cudaEventRecord(e1, s);
-    if (cudaEventSynchronize(e1) != cudaSuccess) return -1.f;
-    float ms = 0;
-    cudaEventElapsedTime(&ms, e0, e1);
-    return ms / reps;
+    return time_runs(m->ctx->event(0), m->ctx->event(1), s, reps,
+                     [&]() { return enqueue_trlwe(m, d_in, il, d_out, ol, s); });
 }
 
 float time_candidate_lwe(idash_model *m, uint32_t n_indiv, const int32_t *d_in, uint64_t in_stride, uint64_t o_lo,
                          uint64_t o_hi, int32_t *d_out, uint64_t out_stride, cudaStream_t s, int reps) {
-    cudaEvent_t e0 = m->ctx->event(0), e1 = m->ctx->event(1);
     const uint32_t rw = row_words_of(m, n_indiv);
     auto run = [&]() {
         return launch_phases(m, o_lo, o_hi, s, [&](uint32_t lo, uint32_t hi) {
@@ -298,15 +313,7 @@ float time_candidate_lwe(idash_model *m, uint32_t n_indiv, const int32_t *d_in, 
                              reinterpret_cast<uint8_t *>(d_out), out_stride * 4, rw, lo, hi, o_lo, o_hi, o_lo);
         });
     };
-    if (run() != IDASH_OK) return -1.f;
-    cudaEventRecord(e0, s);
-    for (int r = 0; r < reps; ++r)
-        if (run() != IDASH_OK) return -1.f;
-    cudaEventRecord(e1, s);
-    if (cudaEventSynchronize(e1) != cudaSuccess) return -1.f;
-    float ms = 0;
-    cudaEventElapsedTime(&ms, e0, e1);
-    return ms / reps;
+    return time_runs(m->ctx->event(0), m->ctx->event(1), s, reps, run);
 }
 
 std::vector<Candidate> candidates(idash_model *m) {
@@ -445,7 +452,7 @@ void release_key(StagedKey *k, cudaStream_t s) {
 cudaEvent_t idash_ctx::event(size_t i) {
     while (events.size() <= i) {
         cudaEvent_t e = nullptr;
-        cudaEventCreate(&e);
+        if (cudaEventCreate(&e) != cudaSuccess) return nullptr;  // the caller's timing fails
         events.push_back(e);
     }
     return events[i];
@@ -894,9 +901,7 @@ idash_status idash_score_trlwe_host(idash_model *m, const void *h_in, const idas
             if (s != IDASH_OK) return s;
             ctx->stats.h2d_bytes += (upto - rows_sent) * il->row_stride;
             rows_sent = upto;
-            cudaEvent_t e = ctx->event(ev++);
-            cudaEventRecord(e, ctx->h2d);
-            cudaStreamWaitEvent(ctx->stream, e, 0);
+            if ((s = stream_after(ctx, ctx->stream, ctx->h2d, ev++)) != IDASH_OK) return s;
         }
         if (cb[c + 1] == cb[c]) continue;
         const uint64_t o_lo = m->plan.blocks[cb[c]].out_lo, o_hi = m->plan.blocks[cb[c + 1] - 1].out_hi;
@@ -924,9 +929,7 @@ idash_status idash_score_trlwe_host(idash_model *m, const void *h_in, const idas
         f.out_hdr_off = ol->header_offset;
         f.tag = m->tp.record_tag;
         if ((s = ctx->check_cuda(launch_finalize(f, ctx->stream), "finalize")) != IDASH_OK) return s;
-        cudaEvent_t e = ctx->event(ev++);
-        cudaEventRecord(e, ctx->stream);
-        cudaStreamWaitEvent(ctx->d2h, e, 0);
+        if ((s = stream_after(ctx, ctx->d2h, ctx->stream, ev++)) != IDASH_OK) return s;
         s = ctx->check_cuda(cudaMemcpyAsync(host_out + o_lo * ol->row_stride, d_out + o_lo * ol->row_stride,
                                             (o_hi - o_lo) * ol->row_stride, cudaMemcpyDeviceToHost, ctx->d2h),
                             "d2h chunk");

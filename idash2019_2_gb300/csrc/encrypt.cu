@@ -233,7 +233,8 @@ extern "C" idash_status idash_encrypt_trlwe_device(idash_ctx *ctx, const idash_e
         const size_t smem = (size_t(neg_mask_words(p->N)) + size_t(rows_per_cta) * neg_ext_words(p->N)) * 4;
         auto launch = [&](auto kernel) {
             // up to 8 rows of 2.25N words (144 KiB at N = 2048): above the default 48 KiB
-            cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+            const cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+            if (e != cudaSuccess) return e;
             int per_sm = 0;
             if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kEncThreads, smem) != cudaSuccess ||
                 per_sm < 1)
@@ -241,13 +242,12 @@ extern "C" idash_status idash_encrypt_trlwe_device(idash_ctx *ctx, const idash_e
             const uint64_t ctas = (n_rows + rows_per_cta - 1) / rows_per_cta;
             const uint32_t blocks = uint32_t(std::min<uint64_t>(ctas, uint64_t(ctx->sm_count) * per_sm));
             kernel<<<blocks, kEncThreads, smem, s>>>(a);
+            return cudaGetLastError();
         };
-        switch (row_threads) {
-            case 32: launch(k_encrypt_binary<32>); break;
-            case 64: launch(k_encrypt_binary<64>); break;
-            default: launch(k_encrypt_binary<128>); break;
-        }
-        st = ctx->check_cuda(cudaGetLastError(), "k_encrypt_binary launch");
+        const cudaError_t le = row_threads == 32   ? launch(k_encrypt_binary<32>)
+                               : row_threads == 64 ? launch(k_encrypt_binary<64>)
+                                                   : launch(k_encrypt_binary<128>);
+        st = ctx->check_cuda(le, "k_encrypt_binary launch");
         release_key(&k, s);
         if (st == IDASH_OK) ctx->stats.kernel_launches++;
         return st;

@@ -770,7 +770,7 @@ extern "C" idash_status idash_score_intpoly_device(idash_model *m, const void *d
     cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
     idash_status s = IDASH_OK;
     if (ip.c_hat_rows < ip.n_rows) {
-        cudaStreamSynchronize(st);
+        if ((s = ctx->check_cuda(cudaStreamSynchronize(st), "sync before growing C^")) != IDASH_OK) return s;
         cudaFree(ip.d_c_hat);
         ip.d_c_hat = nullptr;
         ip.c_hat_rows = 0;

@@ -165,7 +165,8 @@ extern "C" idash_status idash_serve_trlwe(idash_model *m, const idash_serve_conf
             if (q == cudaErrorNotReady) continue;
             if ((st = ctx->check_cuda(q, "request completion")) != IDASH_OK) break;
             float ms = 0;
-            cudaEventElapsedTime(&ms, t0_evt, s.done);
+            if ((st = ctx->check_cuda(cudaEventElapsedTime(&ms, t0_evt, s.done), "completion time")) != IDASH_OK)
+                break;
             idash_request_result &res = results[s.req];
             res.done_s = ms * 1e-3;
             res.device_bytes = s.bytes;
