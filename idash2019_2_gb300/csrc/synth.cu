@@ -147,11 +147,19 @@ __global__ void k_digest(const uint32_t *words, uint64_t n_words, uint64_t index
 __global__ void k_fill_uniform(uint64_t seed, uint64_t row_begin, uint64_t n_rows, uint32_t row_words,
                                uint8_t *base, uint64_t stride) {
     const uint64_t key = stream_key(seed, 7);
+    // 16-byte stores of 4 words when every row starts 16-byte aligned
+    const bool quads = ((reinterpret_cast<uintptr_t>(base) | stride) & 15u) == 0 && row_words % 4 == 0;
     // a row per block (grid-stride), its words across the threads: no division
     for (uint64_t r = blockIdx.x; r < n_rows; r += gridDim.x) {
         uint32_t *out = reinterpret_cast<uint32_t *>(base + r * stride);
         const uint64_t w0 = (row_begin + r) * row_words;
-        for (uint32_t j = threadIdx.x; j < row_words; j += blockDim.x) out[j] = hash32k(key, w0 + j);
+        if (quads) {
+            for (uint32_t j = 4 * threadIdx.x; j < row_words; j += 4 * blockDim.x)
+                *reinterpret_cast<uint4 *>(out + j) = make_uint4(hash32k(key, w0 + j), hash32k(key, w0 + j + 1),
+                                                                 hash32k(key, w0 + j + 2), hash32k(key, w0 + j + 3));
+        } else {
+            for (uint32_t j = threadIdx.x; j < row_words; j += blockDim.x) out[j] = hash32k(key, w0 + j);
+        }
     }
 }
 

@@ -74,6 +74,36 @@ def test_fused_digest_of_the_warp_specialised_kernel(served, slice_words):
         assert d == res2[j]["digest"] == res[i]["digest"]
 
 
+def _mix64(z):
+    z = z + np.uint64(0x9E3779B97F4A7C15)
+    z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+    z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+    return z ^ (z >> np.uint64(31))
+
+
+@pytest.mark.parametrize("row_words,stride,offset", [(2048, 8192, 0), (2046, 8196, 0), (2048, 8192, 4)])
+def test_uniform_rows_restate_on_the_host(served, row_words, stride, offset):
+    """The request ciphertext generator (16-byte stores on 16-byte aligned
+    rows, 4-byte stores otherwise) against a numpy restatement: word j of
+    global row r is the high half of mix64(key ^ (r * row_words + j)), with
+    key = mix64(seed + mix64(7))."""
+    ctx = served[0]
+    seed, row_begin, n_rows = 0x1234567890ABCDEF, 37, 5
+    d = ctx.device_alloc(n_rows * stride + 16)
+    d.zero()
+    gpu.synth_uniform_device(ctx, seed, row_begin, n_rows, row_words, d.ptr + offset, stride)
+    ctx.sync()
+    raw = d.download(dtype=np.uint8)[offset:offset + n_rows * stride].view(np.uint32).reshape(n_rows, stride // 4)
+    d.free()
+    with np.errstate(over="ignore"):
+        key = _mix64(np.uint64(seed) + _mix64(np.uint64(7)))
+        idx = (np.arange(row_begin, row_begin + n_rows, dtype=np.uint64)[:, None] * np.uint64(row_words) +
+               np.arange(row_words, dtype=np.uint64)[None, :])
+        want = (_mix64(key ^ idx) >> np.uint64(32)).astype(np.uint32)
+    np.testing.assert_array_equal(raw[:, :row_words], want)
+    assert not raw[:, row_words:].any()  # the stride's padding is untouched
+
+
 def test_the_mix_overlaps_requests(served):
     ctx, w, m, reqs, res, outs = served
     spans = sorted((r["admit_s"], r["done_s"]) for r in res)
