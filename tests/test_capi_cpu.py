@@ -77,3 +77,31 @@ def test_synth_model_rejects_bad_spec(lib):
     spec.n_tags = 0
     m = _lib.SynthModel()
     assert lib.idash_synth_model(C.byref(spec), C.byref(m)) == 1
+
+
+def _word_hash(index, w):
+    """The serving digest's word hash restated in numpy (32-bit lanes): key =
+    lo(index) * 0x85EBCA77 + hi(index) * 0xC2B2AE3D, x = w + key, then
+    x ^= x >> 15, x *= 0x2C1B3C6D, x ^= x >> 12."""
+    index = np.asarray(index, np.uint64)
+    lo = (index & np.uint64(0xFFFFFFFF)).astype(np.uint32)
+    hi = (index >> np.uint64(32)).astype(np.uint32)
+    x = np.asarray(w, np.uint32) + lo * np.uint32(0x85EBCA77) + hi * np.uint32(0xC2B2AE3D)
+    x ^= x >> np.uint32(15)
+    x *= np.uint32(0x2C1B3C6D)
+    x ^= x >> np.uint32(12)
+    return x
+
+
+@pytest.mark.parametrize("index_base", [0, 1 << 20, (1 << 32) - 5, 3 << 33])
+def test_digest_host_restates_the_word_hash(lib, index_base):
+    """idash_digest_host (the host restatement the serving tests check the
+    device digests against) is the sum mod 2^64 of the word hash, including
+    where the index crosses 2^32."""
+    import ctypes as C
+    words = np.random.default_rng(index_base % 1000).integers(0, 2 ** 32, 1000, dtype=np.uint64).astype(np.uint32)
+    with np.errstate(over="ignore"):
+        h = _word_hash(np.uint64(index_base) + np.arange(words.size, dtype=np.uint64), words)
+    want = int(h.astype(np.uint64).sum(dtype=np.uint64))
+    got = lib.idash_digest_host(words.ctypes.data_as(C.POINTER(C.c_uint32)), words.size, index_base)
+    assert got == want
