@@ -48,7 +48,10 @@ int main(int argc, char **argv) {
     if (cached) std::cout << "model from cache: " << cache_env << std::endl;
     const double t_start = wall();
     CloudTiming tm;
+    const std::string cache_path = cache_env ? cache_env : "";
+    const bool plan_cached = st.ok() && apply_cached_plan(ctx, cache_path, "params.bin", model_dir);
     if (st.ok()) st = cloud_compute_score(preds, data, flat, params, ctx, &tm);
+    if (st.ok() && !plan_cached) save_plan(cache_path, "params.bin", model_dir, tm.plan);
     const double t_end = wall();
     if (st.ok()) st = write_encrypted_predictions(preds, "encrypted_prediction.bin");
     const double t_write = wall();

@@ -422,6 +422,40 @@ Status read_model_cache(FlatModel *flat, uint64_t fp, const std::string &path) {
     return Status::Ok();
 }
 
+namespace {
+constexpr char kPlanMagic[8] = {'I', 'D', 'G', 'P', 'L', 'A', 'N', '1'};
+// idash_model_info::kernel (0 window, 1 direct, 2 pipe, 3 warp-specialised)
+// as the "kernel" option's value (2, 1, 3, 4)
+constexpr int64_t kKernelOption[4] = {2, 1, 3, 4};
+}  // namespace
+
+bool apply_cached_plan(idash_ctx *ctx, const std::string &cache_path, const std::string &params_file,
+                       const std::string &model_dir) {
+    if (cache_path.empty()) return false;
+    FILE *f = std::fopen((cache_path + ".plan").c_str(), "rb");
+    if (!f) return false;
+    char magic[8];
+    uint64_t rec[3];
+    const bool ok = std::fread(magic, 1, 8, f) == 8 && std::memcmp(magic, kPlanMagic, 8) == 0 &&
+                    std::fread(rec, 8, 3, f) == 3;
+    std::fclose(f);
+    if (!ok || rec[0] != fingerprint(params_file, model_dir) || rec[1] > 3) return false;
+    return idash_set_option(ctx, "kernel", kKernelOption[rec[1]]) == IDASH_OK &&
+           idash_set_option(ctx, "slice_words", int64_t(rec[2])) == IDASH_OK;
+}
+
+void save_plan(const std::string &cache_path, const std::string &params_file, const std::string &model_dir,
+               const idash_model_info &plan) {
+    if (cache_path.empty() || plan.kernel > 3 || plan.slice_words == 0) return;
+    const std::string path = cache_path + ".plan", tmp = path + ".tmp";
+    FILE *f = std::fopen(tmp.c_str(), "wb");
+    if (!f) return;
+    const uint64_t rec[3] = {fingerprint(params_file, model_dir), plan.kernel, plan.slice_words};
+    bool ok = std::fwrite(kPlanMagic, 1, 8, f) == 8 && std::fwrite(rec, 8, 3, f) == 3;
+    ok = (std::fclose(f) == 0) && ok;
+    if (!ok || std::rename(tmp.c_str(), path.c_str()) != 0) std::remove(tmp.c_str());
+}
+
 Status load_model(Model *parsed, FlatModel *flat, const IdashParams &params, const std::string &params_file,
                   const std::string &model_dir, const std::string &cache_path, bool *from_cache) {
     *from_cache = false;
@@ -486,6 +520,7 @@ Status cloud_compute_score(EncryptedPredictions &preds, const EncryptedData &dat
     Status st = s == IDASH_OK ? Status::Ok() : Status::Err(s, idash_last_error(ctx));
     if (d_in) idash_device_free(ctx, d_in);
     if (d_out) idash_device_free(ctx, d_out);
+    if (st.ok() && timing) idash_model_get_info(m, &timing->plan);
     idash_model_free(m);
     if (!st.ok()) return st;
     std::memcpy(preds.image.data, &preds.image.count, 8);
@@ -528,7 +563,10 @@ extern "C" idash_status idash_cloud_files(int device, const char *params_file, c
     idash_ctx *ctx = nullptr;
     idash_status s = idash_open(&ctx, device);
     if (s != IDASH_OK) return fail(Status::Err(s, idash_last_error(nullptr)));
+    const std::string cache_path = cache_env ? cache_env : "";
+    const bool plan_cached = apply_cached_plan(ctx, cache_path, params_file, model_dir);
     if (st.ok()) st = cloud_compute_score(preds, data, flat, params, ctx, &tm);
+    if (st.ok() && !plan_cached) save_plan(cache_path, params_file, model_dir, tm.plan);
     const double t2 = now_s();
     if (st.ok()) st = write_encrypted_predictions(preds, pred_file);
     const double t3 = now_s();

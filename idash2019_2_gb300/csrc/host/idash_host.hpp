@@ -97,7 +97,18 @@ Status read_encrypted_predictions(EncryptedPredictions &preds, const std::string
 
 struct CloudTiming {
     double plan_s = 0, score_s = 0;  // model planning; copies + kernels
+    idash_model_info plan{};         // the plan the scoring ran (kernel kind, slice width)
 };
+
+// The tuned plan beside a model cache (`<cache>.plan`), keyed by the same
+// fingerprint: apply_cached_plan pins its kernel kind and slice width on the
+// context before the model is planned, so the autotuner only chooses among
+// what is left (ring depth, CTAs per SM); save_plan records it after a run.
+// Both are best effort: a missing or stale file changes nothing.
+bool apply_cached_plan(idash_ctx *ctx, const std::string &cache_path, const std::string &params_file,
+                       const std::string &model_dir);
+void save_plan(const std::string &cache_path, const std::string &params_file, const std::string &model_dir,
+               const idash_model_info &plan);
 
 // The model as the GPU consumes it: outputs in FeatBigIndex order (so that
 // neighbouring targets share input windows), each output's terms in the

@@ -62,12 +62,24 @@ def test_model_cache_is_written_then_used(tmp_path, monkeypatch):
     flattened model; the second reads it; both outputs equal the reference's."""
     src = copy_case("ref_r3_edge", tmp_path)
     monkeypatch.setenv("IDASH_MODEL_CACHE", str(tmp_path / "model.cache"))
+    plan = tmp_path / "model.cache.plan"
     for expect_cached in (0, 1):
         out = tmp_path / f"pred{expect_cached}.bin"
         rep = gpu.cloud_files(str(tmp_path / "params.bin"), str(tmp_path / "model"),
                               str(tmp_path / "encrypted_data.bin"), str(out))
         assert rep["model_from_cache"] == expect_cached
         assert filecmp.cmp(out, os.path.join(src, "encrypted_prediction.bin"), shallow=False)
+        # the first run records the tuned plan (magic, fingerprint, kernel kind, slice width)
+        raw = plan.read_bytes()
+        assert len(raw) == 32 and raw[:8] == b"IDGPLAN1"
+        kind, slice_words = np.frombuffer(raw[16:], np.uint64)
+        assert kind <= 3 and slice_words in (128, 256, 512, 1024, 2048)
+    # a damaged plan file is ignored and replaced
+    plan.write_bytes(b"IDGPLAN1" + b"\xff" * 24)
+    rep = gpu.cloud_files(str(tmp_path / "params.bin"), str(tmp_path / "model"),
+                          str(tmp_path / "encrypted_data.bin"), str(tmp_path / "pred_p.bin"))
+    assert filecmp.cmp(tmp_path / "pred_p.bin", os.path.join(src, "encrypted_prediction.bin"), shallow=False)
+    assert plan.read_bytes()[8:16] != b"\xff" * 8
     # a cache for other params is ignored (and replaced)
     (tmp_path / "params2.bin").write_bytes((tmp_path / "params.bin").read_bytes())
     rep = gpu.cloud_files(str(tmp_path / "params2.bin"), str(tmp_path / "model"),
