@@ -8,9 +8,13 @@
 //   -Dcloud_compute_score=cloud_compute_score_cpu
 // (or delete its definition), add this file, and link libidash_gpu.so.
 // Behaviour kept: enc_preds gets one new TLweSample per model output
-// (createAndGet, eval/idash.h:174-183), coefficients and current_variance as
-// the reference computes them; failures print and abort like
-// REQUIRE_DRAMATICALLY (eval/idash.h:12).
+// (createAndGet, eval/idash.h:174-183), created in the model map's iteration
+// order before any scoring, as eval/idash.cpp:772-777 creates them.  The
+// order of insertion decides the iteration order of enc_preds.score, and so
+// the record order write_encrypted_predictions writes (eval/idash.cpp:605-608):
+// the prediction file comes out byte-identical to the reference's.
+// Coefficients and current_variance are the reference's; failures print and
+// abort like REQUIRE_DRAMATICALLY (eval/idash.h:12).
 #include <algorithm>
 #include <cstring>
 #include <vector>
@@ -19,8 +23,6 @@
 #include "idash_gpu.h"
 
 namespace {
-
-constexpr uint64_t kStride = 8 + 2 * 1024 * 4 + 8;  // one record: index, tag, a|b, variance
 
 void require_ok(idash_status s, idash_ctx *ctx, const char *what) {
     if (s != IDASH_OK) {
@@ -43,11 +45,19 @@ void cloud_compute_score(EncryptedPredictions &enc_preds, const EncryptedData &e
     const TLweParams *tp = params.tlweParams;
     REQUIRE_DRAMATICALLY(tp->k == 1 && tp->N == (int32_t)params.N, "only k = 1, N = IdashParams::N");
     const uint32_t N = params.N;
+    const uint64_t kStride = 16 + 8 * uint64_t(N);  // one record: index, tag, a|b, variance
     idash_ctx *ctx = context();
 
-    // Outputs in FeatBigIndex order, terms in the model map's iteration order.
+    // The output samples first, in the model map's iteration order
+    // (eval/idash.cpp:772-777): this fixes the record order of the file.
     std::vector<FeatBigIndex> outs;
-    for (const auto &it : model.model) outs.push_back(it.first);
+    for (const auto &it : model.model) {
+        enc_preds.createAndGet(it.first, tp);
+        outs.push_back(it.first);
+    }
+    // Scored in FeatBigIndex order (neighbouring targets share input
+    // windows), terms in each inner map's iteration order (the order of the
+    // double variance sum, eval/idash.cpp:800-819).
     std::sort(outs.begin(), outs.end());
     std::vector<uint64_t> term_ptr(outs.size() + 1, 0);
     std::vector<uint32_t> term_feat;
@@ -92,7 +102,7 @@ void cloud_compute_score(EncryptedPredictions &enc_preds, const EncryptedData &e
     idash_model_free(m);
 
     for (size_t o = 0; o < outs.size(); ++o) {
-        TLweSample *s = enc_preds.createAndGet(outs[o], tp);
+        TLweSample *s = enc_preds.get(outs[o], tp);
         const uint8_t *rec = out + o * kStride;
         std::memcpy(s->a[0].coefsT, rec + 8, sizeof(Torus32) * N);
         std::memcpy(s->b->coefsT, rec + 8 + 4 * N, sizeof(Torus32) * N);

@@ -24,8 +24,6 @@
 
 namespace {
 
-constexpr uint64_t kStride = 8 + 2 * 1024 * 4 + 8;  // one record: index, tag, a|b, variance
-
 void require_ok(idash_status s, idash_ctx *ctx, const char *what) {
     if (s != IDASH_OK) {
         std::cout << "ERROR: " << what << ": " << idash_status_string(s) << ": " << idash_last_error(ctx)
@@ -46,6 +44,7 @@ void decrypt_predictions(DecryptedPredictions &predictions, const EncryptedPredi
                          const IdashKey &key) {
     const IdashParams &params = *key.idashParams;
     const uint32_t N = params.N, NS = params.NUM_SAMPLES;
+    const uint64_t kStride = 16 + 8 * uint64_t(N);  // one record: index, tag, a|b, variance
     REQUIRE_DRAMATICALLY(key.tlweKey->params->k == 1 && key.tlweKey->params->N == (int32_t)N,
                          "only k = 1, N = IdashParams::N");
     idash_ctx *ctx = context();
@@ -87,6 +86,7 @@ void decrypt_predictions(DecryptedPredictions &predictions, const EncryptedPredi
 void encrypt_data_ph1(EncryptedData &enc_data, const PlaintextData &plain_data, const IdashKey &key) {
     const IdashParams &params = *key.idashParams;
     const uint32_t N = params.N;
+    const uint64_t kStride = 16 + 8 * uint64_t(N);  // one record: index, tag, a|b, variance
     REQUIRE_DRAMATICALLY(plain_data.data.size() == params.NUM_INPUT_POSITIONS, "Incomplete plaintext");
     REQUIRE_DRAMATICALLY(key.tlweKey->params->k == 1 && key.tlweKey->params->N == (int32_t)N,
                          "only k = 1, N = IdashParams::N");

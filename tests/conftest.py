@@ -9,6 +9,10 @@ for p in (ROOT, os.path.join(ROOT, "oracle"), os.path.join(ROOT, "tests", "golde
         sys.path.insert(0, p)
 
 GOLDEN = os.path.join(ROOT, "tests", "golden")
+# The reference checkout (sources only; never needed on a GPU machine): REF_DIR,
+# else a directory named "reference" beside the repository.
+REF_DIR = os.environ.get("REF_DIR") or os.path.join(os.path.dirname(ROOT), "reference")
+HAVE_REF = os.path.isdir(os.path.join(REF_DIR, "eval"))
 SMALL_CASES = ["ref_r10", "ref_r1", "ref_r3_edge"]
 
 

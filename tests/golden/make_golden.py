@@ -1,6 +1,6 @@
 """Regenerates the golden fixtures from the reference's own pipeline.
 
-Needs the reference sources (default /root/reference, or REF_DIR) and builds
+Needs the reference sources (REF_DIR, else "reference" beside the repository) and builds
 them with `make -C oracle ref` (the reference's eval/*.cpp compiled against
 oracle/tfhe_compat).  Run from the repository root:
 
@@ -115,7 +115,7 @@ def make_hashed():
 
 
 def main():
-    ref = os.environ.get("REF_DIR", "/root/reference")
+    ref = os.environ.get("REF_DIR") or os.path.join(os.path.dirname(ROOT), "reference")
     run(["make", "-s", "ref", f"REF_DIR={ref}"], os.path.join(ROOT, "oracle"))
     if "--named-csv" in sys.argv:  # only add result.csv to the committed cases
         for name in SMALL_CASES:
