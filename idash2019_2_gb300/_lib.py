@@ -160,8 +160,9 @@ PROTOTYPES = {
     "idash_model_get_info": (status_t, [vp, C.POINTER(ModelInfo)]),
     "idash_model_replan": (status_t, [vp]),
     "idash_model_free": (None, [vp]),
-    "idash_score_trlwe_noalloc": (status_t, [C.POINTER(TrlweParams), C.c_uint64, u64p, u32p, i32p, C.c_uint64,
-                                             vp, C.POINTER(RowLayout), vp, C.POINTER(RowLayout), vp]),
+    "idash_score_trlwe_noalloc": (status_t, [C.POINTER(TrlweParams), C.c_uint64, u32p, u64p, u32p, i32p,
+                                             C.c_uint64, u32p, C.c_uint64, vp, C.POINTER(RowLayout), vp,
+                                             C.POINTER(RowLayout), vp]),
     "idash_cloud_files": (status_t, [C.c_int, C.c_char_p, C.c_char_p, C.c_char_p, C.c_char_p,
                                      C.POINTER(CloudReport), C.c_char_p, C.c_size_t]),
     "idash_encrypt_trlwe_device": (status_t, [vp, C.POINTER(EncryptParams), i32p, C.c_uint64, C.c_uint64, vp,

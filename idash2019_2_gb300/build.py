@@ -35,6 +35,7 @@ LIB_SOURCES = [
     "csrc/score_kernels.cu",
     "csrc/synth.cu",
     "csrc/noalloc.cu",
+    "csrc/noalloc_plan.cpp",
     "csrc/intpoly.cu",
     "csrc/server.cpp",
     "csrc/capi.cpp",

@@ -8,28 +8,28 @@
 // cudaMalloc/cudaFree.  They still own the input and output buffers.  This
 // entry point needs nothing else from the device heap.  Its scratch is the
 // array below: the planned work list (blocks, slots, groups, terms), the
-// window kernel's tile counter, the device error word and the variance
-// program.  The array is a fixed part of the library's device image, so every
-// GPU that loads the library holds it until the process exits.
+// window kernel's tile counter, the device error word, the variance program
+// and the output index table (noalloc_plan.cpp lays them out).  The array is
+// a fixed part of the library's device image, so every GPU that loads the
+// library holds it until the process exits.
 #include <cstring>
 #include <mutex>
 #include <string>
 #include <vector>
 
 #include "capi_internal.hpp"
+#include "noalloc_plan.hpp"
 
 namespace {
 
-// 32 MiB per device: enough for the full-scale model (242,646 outputs,
-// 5 neighbours) with room to spare.  Larger models are refused.
-constexpr size_t kScratchBytes = size_t(32) << 20;
-static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
+// kNoallocScratchBytes (64 MiB) per device: the full-scale model (242,646
+// outputs, 5 neighbours) fits in the reference's record layout with its
+// variance program.  Larger models are refused.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[idash::kNoallocScratchBytes];
 
 constexpr int kMaxDevices = 64;
 std::mutex g_setup_mutex;
 unsigned char *g_scratch_addr[kMaxDevices] = {};  // device address per device, set on first call
-
-size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
 idash_status fail(idash_status s, const std::string &msg) {
     idash_set_thread_error(msg);
@@ -72,8 +72,10 @@ bool layout_ok(const void *base, const idash_row_layout *l, uint64_t payload) {
 
 }  // namespace
 
-extern "C" idash_status idash_score_trlwe_noalloc(const idash_trlwe_params *p, uint64_t n_out, const uint64_t *term_ptr,
+extern "C" idash_status idash_score_trlwe_noalloc(const idash_trlwe_params *p, uint64_t n_out,
+                                                  const uint32_t *out_index, const uint64_t *term_ptr,
                                                   const uint32_t *term_feat, const int32_t *term_coef,
+                                                  uint64_t n_in_index, const uint32_t *in_row_of_index,
                                                   uint64_t n_in_rows, const void *d_in,
                                                   const idash_row_layout *in_layout, void *d_out,
                                                   const idash_row_layout *out_layout, void *stream) {
@@ -81,6 +83,7 @@ extern "C" idash_status idash_score_trlwe_noalloc(const idash_trlwe_params *p, u
     if (!p || !d_in || !d_out || !in_layout || !out_layout || (n_out && (!term_ptr || (term_ptr[n_out] &&
                                                                                       (!term_feat || !term_coef)))))
         return fail(IDASH_ERR_INVALID_ARGUMENT, "null argument");
+    if (n_in_index && !in_row_of_index) return fail(IDASH_ERR_INVALID_ARGUMENT, "n_in_index without in_row_of_index");
     if (p->k != 1 || p->N == 0 || p->N % 256 || p->N > 4096)
         return fail(IDASH_ERR_UNSUPPORTED, "need k = 1 and N a multiple of 256 up to 4096");
     if (p->num_regions == 0 || p->region_size == 0 || uint64_t(p->num_regions) * p->region_size > p->N ||
@@ -101,8 +104,7 @@ extern "C" idash_status idash_score_trlwe_noalloc(const idash_trlwe_params *p, u
     idash_status s = setup_device(dev, &scratch, &sm_count, &smem_optin);
     if (s != IDASH_OK) return s;
 
-    // Plan on the host (ordinary heap memory): the window kernel with the
-    // widest slice whose window holds every output's slots, 2 CTAs per SM.
+    // Plan on the host (ordinary heap memory).
     PlanInput in;
     in.form = Form::kTrlwe;
     in.n_out = n_out;
@@ -113,79 +115,45 @@ extern "C" idash_status idash_score_trlwe_noalloc(const idash_trlwe_params *p, u
     in.N = p->N;
     in.num_regions = p->num_regions;
     in.region_size = p->region_size;
+    in.row_of_index = in_row_of_index;
+    in.n_index = in_row_of_index ? n_in_index : 0;
     in.n_rows = n_in_rows;
-    Plan plan;
-    KernelKind kind = KernelKind::kDirect;
-    uint32_t w = 512, g = 1;
-    std::string err;
-    bool index_error = false;
-    for (uint32_t cand : {1024u, 512u, 256u}) {
-        const size_t budget = std::min<size_t>(233472 / 2 - 1024, smem_optin);
-        PlanLimits lim;
-        lim.group_size = 3;
-        lim.max_groups = 64;
-        lim.max_terms = uint32_t((budget - 128 - 64 * sizeof(PlanGroup)) / 4 / sizeof(PlanTerm));
-        lim.max_slots = uint32_t((budget - 128 - 64 * sizeof(PlanGroup) - lim.max_terms * sizeof(PlanTerm)) /
-                                 (size_t(cand) * 4));
-        err = build_plan(in, lim, &plan, &index_error);
-        if (err.empty()) {
-            kind = KernelKind::kWindow;
-            w = cand;
-            g = 3;
-            break;
-        }
-        if (index_error) return fail(IDASH_ERR_INDEX, err);
-    }
-    if (kind == KernelKind::kDirect) {
-        PlanLimits lim;
-        lim.group_size = 1;
-        lim.max_slots = lim.max_terms = 0xFFFFFFFFu;
-        lim.max_groups = 8;
-        err = build_plan(in, lim, &plan, &index_error);
-        if (!err.empty()) return fail(index_error ? IDASH_ERR_INDEX : IDASH_ERR_UNSUPPORTED, err);
-    }
-
-    // Carve the scratch: error word + tile counter, then the tables.
     const bool want_var = out_layout->variance_offset >= 0;
-    size_t off = 256;
-    auto take = [&](size_t bytes) {
-        const size_t at = off;
-        off = align256(off + std::max<size_t>(bytes, 1));
-        return at;
-    };
-    const size_t o_blocks = take(plan.blocks.size() * sizeof(PlanBlock));
-    const size_t o_slots = take(plan.slots.size() * sizeof(PlanSlot));
-    const size_t o_groups = take(plan.groups.size() * sizeof(PlanGroup));
-    const size_t o_terms = take(plan.terms.size() * sizeof(PlanTerm));
-    const size_t o_vptr = want_var ? take(plan.var_ptr.size() * 8) : 0;
-    const size_t o_vrow = want_var ? take(plan.var_row.size() * 4) : 0;
-    const size_t o_vcoef = want_var ? take(plan.var_coef.size() * 4) : 0;
-    if (off > kScratchBytes)
-        return fail(IDASH_ERR_INVALID_ARGUMENT, "model needs " + std::to_string(off >> 20) +
-                                                    " MiB of scratch; the no-allocation entry point holds 32 MiB");
+    const bool want_index = out_index && out_layout->header_offset >= 0;
+    NoallocPlan np;
+    bool index_error = false;
+    const std::string err = plan_noalloc(in, smem_optin, want_var, want_index, &np, &index_error);
+    if (!err.empty())
+        return fail(index_error ? IDASH_ERR_INDEX : np.bytes > kNoallocScratchBytes ? IDASH_ERR_INVALID_ARGUMENT
+                                                                                    : IDASH_ERR_UNSUPPORTED,
+                    err);
+    const Plan &plan = np.plan;
 
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     auto put = [&](size_t at, const void *src, size_t bytes) -> cudaError_t {
         return bytes ? cudaMemcpyAsync(scratch + at, src, bytes, cudaMemcpyHostToDevice, st) : cudaSuccess;
     };
     ce = cudaMemsetAsync(scratch, 0, 256, st);  // error word and tile counter start at zero
-    if (ce == cudaSuccess) ce = put(o_blocks, plan.blocks.data(), plan.blocks.size() * sizeof(PlanBlock));
-    if (ce == cudaSuccess) ce = put(o_slots, plan.slots.data(), plan.slots.size() * sizeof(PlanSlot));
-    if (ce == cudaSuccess) ce = put(o_groups, plan.groups.data(), plan.groups.size() * sizeof(PlanGroup));
-    if (ce == cudaSuccess) ce = put(o_terms, plan.terms.data(), plan.terms.size() * sizeof(PlanTerm));
+    if (ce == cudaSuccess) ce = put(np.o_blocks, plan.blocks.data(), plan.blocks.size() * sizeof(PlanBlock));
+    if (ce == cudaSuccess) ce = put(np.o_slots, plan.slots.data(), plan.slots.size() * sizeof(PlanSlot));
+    if (ce == cudaSuccess) ce = put(np.o_groups, plan.groups.data(), plan.groups.size() * sizeof(PlanGroup));
+    if (ce == cudaSuccess) ce = put(np.o_terms, plan.terms.data(), plan.terms.size() * sizeof(PlanTerm));
     if (ce == cudaSuccess && want_var) {
-        ce = put(o_vptr, plan.var_ptr.data(), plan.var_ptr.size() * 8);
-        if (ce == cudaSuccess) ce = put(o_vrow, plan.var_row.data(), plan.var_row.size() * 4);
-        if (ce == cudaSuccess) ce = put(o_vcoef, plan.var_coef.data(), plan.var_coef.size() * 4);
+        ce = put(np.o_var_ptr, plan.var_ptr.data(), plan.var_ptr.size() * 8);
+        if (ce == cudaSuccess) ce = put(np.o_var_row, plan.var_row.data(), plan.var_row.size() * 4);
+        if (ce == cudaSuccess) ce = put(np.o_var_coef, plan.var_coef.data(), plan.var_coef.size() * 4);
     }
+    if (ce == cudaSuccess && want_index) ce = put(np.o_out_index, out_index, n_out * 4);
     if (ce != cudaSuccess) return fail(IDASH_ERR_CUDA, std::string("scratch upload: ") + cudaGetErrorString(ce));
 
     uint32_t *d_err = reinterpret_cast<uint32_t *>(scratch);
+    const KernelKind kind = np.window ? KernelKind::kWindow : KernelKind::kDirect;
+    const uint32_t w = np.slice_words, g = np.group_size;
     ScoreArgs a{};
-    a.blocks = reinterpret_cast<const PlanBlock *>(scratch + o_blocks);
-    a.slots = reinterpret_cast<const PlanSlot *>(scratch + o_slots);
-    a.groups = reinterpret_cast<const PlanGroup *>(scratch + o_groups);
-    a.terms = reinterpret_cast<const PlanTerm *>(scratch + o_terms);
+    a.blocks = reinterpret_cast<const PlanBlock *>(scratch + np.o_blocks);
+    a.slots = reinterpret_cast<const PlanSlot *>(scratch + np.o_slots);
+    a.groups = reinterpret_cast<const PlanGroup *>(scratch + np.o_groups);
+    a.terms = reinterpret_cast<const PlanTerm *>(scratch + np.o_terms);
     a.block_lo = 0;
     a.n_blocks = uint32_t(plan.blocks.size());
     a.row_words = 2 * p->N;
@@ -218,10 +186,10 @@ extern "C" idash_status idash_score_trlwe_noalloc(const idash_trlwe_params *p, u
     ce = launch_score(kind, w, g, a, ctas, st);
     if (ce == cudaSuccess && (out_layout->variance_offset >= 0 || out_layout->header_offset >= 0)) {
         FinalizeArgs f{};
-        f.var_ptr = reinterpret_cast<const uint64_t *>(scratch + o_vptr);
-        f.var_row = reinterpret_cast<const uint32_t *>(scratch + o_vrow);
-        f.var_coef = reinterpret_cast<const int32_t *>(scratch + o_vcoef);
-        f.out_index = nullptr;
+        f.var_ptr = reinterpret_cast<const uint64_t *>(scratch + np.o_var_ptr);
+        f.var_row = reinterpret_cast<const uint32_t *>(scratch + np.o_var_row);
+        f.var_coef = reinterpret_cast<const int32_t *>(scratch + np.o_var_coef);
+        f.out_index = want_index ? reinterpret_cast<const uint32_t *>(scratch + np.o_out_index) : nullptr;
         f.out_row_map = nullptr;
         f.o_begin = 0;
         f.o_end = n_out;

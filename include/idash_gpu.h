@@ -278,11 +278,15 @@ void idash_model_free(idash_model *model);
  * a service whose framework reserves the GPU's memory for its own pool, a
  * process at its per-client device-memory limit, or a latency-bound loop
  * that cannot take the implicit synchronisation of cudaMalloc/cudaFree.  The
- * caller passes the model (host CSR, as idash_model_trlwe) and device input
- * and output rows, as idash_score_trlwe_device (output o -> row o); nothing
- * else comes from the device heap.  The plan, tile counter, error word and
- * variance program live in a fixed 32 MiB array that every GPU loading the
- * library holds until the process exits; a model whose plan does not fit is
+ * caller passes the model as host CSR with the same arguments and meaning as
+ * idash_model_trlwe (out_index: FeatBigIndex per output for record headers,
+ * NULL: o; in_row_of_index: FeatIndex -> input row, NULL: identity), and
+ * device input and output rows as idash_score_trlwe_device (output o -> row
+ * o); nothing else comes from the device heap.  The plan, tile counter, error
+ * word, variance program and output index table live in a fixed 64 MiB array
+ * that every GPU loading the library holds until the process exits (the
+ * full-scale model, 242,646 outputs with 5 neighbours in the reference's
+ * record layout, needs about 52 MiB); a model whose tables do not fit is
  * refused with IDASH_ERR_INVALID_ARGUMENT before anything is launched.
  * Runs on the calling thread's current device, on `stream` (NULL: the legacy
  * default stream), and returns after the outputs are written.  The first call
@@ -292,9 +296,11 @@ void idash_model_free(idash_model *model);
  * cleared by each call): calls that overlap on one GPU, from several threads
  * or streams, race and must be serialised by the caller.  Host-side planning
  * uses ordinary heap memory; no device or page-locked memory is allocated. */
-idash_status idash_score_trlwe_noalloc(const idash_trlwe_params *params, uint64_t n_out, const uint64_t *term_ptr,
-                                       const uint32_t *term_feat, const int32_t *term_coef, uint64_t n_in_rows,
-                                       const void *d_in, const idash_row_layout *in_layout, void *d_out,
+idash_status idash_score_trlwe_noalloc(const idash_trlwe_params *params, uint64_t n_out, const uint32_t *out_index,
+                                       const uint64_t *term_ptr, const uint32_t *term_feat,
+                                       const int32_t *term_coef, uint64_t n_in_index,
+                                       const uint32_t *in_row_of_index, uint64_t n_in_rows, const void *d_in,
+                                       const idash_row_layout *in_layout, void *d_out,
                                        const idash_row_layout *out_layout, void *stream);
 
 /* ------------------------------------------- the cloud step on files
