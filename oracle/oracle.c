@@ -219,3 +219,99 @@ void oracle_synth_lwe_words(uint64_t seed, uint32_t n, uint32_t n_indiv, uint64_
         out[w - w0] = (int32_t)b;
     }
 }
+
+/* ------------------------------------------------------------------ synth */
+static uint64_t synth_key(uint64_t seed, uint64_t stream) { return oracle_mix64(seed + oracle_mix64(stream)); }
+static uint32_t synth_h(uint64_t key, uint64_t index) { return (uint32_t)(oracle_mix64(key ^ index) >> 32); }
+
+static int cmp_u64(const void *a, const void *b) {
+    const uint64_t x = *(const uint64_t *)a, y = *(const uint64_t *)b;
+    return x < y ? -1 : x > y;
+}
+
+void oracle_synth_model_free(oracle_synth_model_t *m) {
+    if (!m) return;
+    free(m->term_ptr);
+    free(m->term_feat);
+    free(m->term_coef);
+    free(m->window_start);
+    free(m->window_len);
+    memset(m, 0, sizeof(*m));
+}
+
+int oracle_synth_model(uint64_t seed, uint32_t n_tags, uint32_t n_targets, uint32_t neighbours, uint32_t n_choices,
+                       const uint32_t *choices, oracle_synth_model_t *out) {
+    memset(out, 0, sizeof(*out));
+    if (n_tags == 0 || (neighbours == 0 && (n_choices == 0 || !choices))) return -1;
+    const uint32_t P = n_tags, T = n_targets;
+    uint64_t *tag = (uint64_t *)malloc(sizeof(uint64_t) * P);
+    uint64_t *tgt = (uint64_t *)malloc(sizeof(uint64_t) * (T + 1));
+    out->window_start = (uint32_t *)malloc(sizeof(uint32_t) * (T + 1));
+    out->window_len = (uint32_t *)malloc(sizeof(uint32_t) * (T + 1));
+    if (!tag || !tgt || !out->window_start || !out->window_len) {
+        free(tag);
+        free(tgt);
+        oracle_synth_model_free(out);
+        return -1;
+    }
+    const uint64_t k10 = synth_key(seed, 10), k11 = synth_key(seed, 11), k12 = synth_key(seed, 12);
+    for (uint32_t p = 0; p < P; ++p) tag[p] = 100 + 16ull * p + synth_h(k10, p) % 16u;
+    const uint64_t lo = tag[0], span = tag[P - 1] - tag[0] + 1;
+    for (uint32_t t = 0; t < T; ++t) tgt[t] = lo + oracle_mix64(k11 ^ t) % span;
+    qsort(tgt, T, sizeof(uint64_t), cmp_u64);
+    uint64_t est = 0;
+    for (uint32_t t = 0; t < T; ++t) {
+        uint32_t k = neighbours ? neighbours : choices[synth_h(k12, t) % n_choices];
+        if (k > P) k = P;
+        /* first tag at or after the target, then grow the window to k tags,
+           taking the left one on ties */
+        int64_t r = 0, hi = P;
+        while (r < hi) {
+            const int64_t mid = (r + hi) / 2;
+            if (tag[mid] < tgt[t]) r = mid + 1;
+            else hi = mid;
+        }
+        int64_t l = r - 1;
+        for (uint32_t got = 0; got < k; ++got) {
+            const int take_left = r >= (int64_t)P || (l >= 0 && tgt[t] - tag[l] <= tag[r] - tgt[t]);
+            if (take_left) --l;
+            else ++r;
+        }
+        out->window_start[t] = (uint32_t)(l + 1);
+        out->window_len[t] = (uint32_t)(r - (l + 1));
+        est += 3ull * (3ull * out->window_len[t] + 1);
+    }
+    free(tag);
+    free(tgt);
+    const uint64_t n_out = 3ull * T;
+    out->term_ptr = (uint64_t *)malloc(sizeof(uint64_t) * (n_out + 1));
+    out->term_feat = (uint32_t *)malloc(sizeof(uint32_t) * (est + 1));
+    out->term_coef = (int32_t *)malloc(sizeof(int32_t) * (est + 1));
+    if (!out->term_ptr || !out->term_feat || !out->term_coef) {
+        oracle_synth_model_free(out);
+        return -1;
+    }
+    const uint64_t kc = synth_key(seed, 13), kb = synth_key(seed, 14);
+    uint64_t nt = 0;
+    out->term_ptr[0] = 0;
+    for (uint64_t o = 0; o < n_out; ++o) {
+        const uint32_t t = (uint32_t)(o / 3);
+        for (uint32_t q = 0; q < out->window_len[t]; ++q) {
+            const uint32_t p = out->window_start[t] + q;
+            for (uint32_t u = 0; u < 3; ++u) {
+                const int32_t c = (int32_t)(synth_h(kc, o * 192 + q * 3 + u) % 16384u) - 8192;
+                if (c == 0) continue;
+                out->term_feat[nt] = 3 * p + u;
+                out->term_coef[nt] = c;
+                ++nt;
+            }
+        }
+        out->term_feat[nt] = ORACLE_CONSTANT_FEATURE;
+        out->term_coef[nt] = (int32_t)(synth_h(kb, o) % 16384u) - 8192;
+        ++nt;
+        out->term_ptr[o + 1] = nt;
+    }
+    out->n_out = n_out;
+    out->n_terms = nt;
+    return 0;
+}

@@ -92,6 +92,30 @@ uint32_t oracle_hash32(uint64_t seed, uint64_t stream, uint64_t index);
 void oracle_synth_lwe_words(uint64_t seed, uint32_t n, uint32_t n_indiv, uint64_t feature,
                             uint64_t w0, uint64_t count, int32_t *out);
 
+/* Seeded synthetic imputation model with the reference's shapes, the same
+ * workload the product's idash_synth_model generates (restated here so that
+ * the CPU reference arm builds its workload from the oracle alone):
+ *   tag p at position 100 + 16p + h(seed, 10, p) % 16;
+ *   targets at sorted positions lo + mix64(key(seed, 11) ^ t) % span;
+ *   target t's neighbours: its k nearest tags, ties to the left
+ *   (train/to_vw.py:33-34), k fixed or choices[h(seed, 12, t) % n_choices];
+ *   outputs 3t..3t+2 (eval/idash.cpp:337-339), features 3p+u of tag p
+ *   (:388-390), coefficient h(key(seed,13), o*192 + q*3 + u) % 16384 - 8192,
+ *   zeros dropped (train/test_vw_hr.py:44), then the constant with
+ *   h(key(seed,14), o) % 16384 - 8192.
+ * Arrays are malloc'd; release with oracle_synth_model_free.  Returns 0, or
+ * -1 on bad arguments / allocation failure. */
+typedef struct {
+    uint64_t n_out, n_terms;
+    uint64_t *term_ptr;
+    uint32_t *term_feat;
+    int32_t *term_coef;
+    uint32_t *window_start, *window_len;
+} oracle_synth_model_t;
+int oracle_synth_model(uint64_t seed, uint32_t n_tags, uint32_t n_targets, uint32_t neighbours, uint32_t n_choices,
+                       const uint32_t *choices, oracle_synth_model_t *out);
+void oracle_synth_model_free(oracle_synth_model_t *m);
+
 #ifdef __cplusplus
 }
 #endif

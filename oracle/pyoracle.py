@@ -55,8 +55,38 @@ def lib() -> C.CDLL:
         L.oracle_synth_lwe_words.argtypes = [C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint64, C.c_uint64,
                                              C.c_uint64, i32p]
         L.oracle_synth_lwe_words.restype = None
+        L.oracle_synth_model.argtypes = [C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, u32p,
+                                         C.POINTER(SynthModel)]
+        L.oracle_synth_model_free.argtypes = [C.POINTER(SynthModel)]
+        L.oracle_synth_model_free.restype = None
         _lib = L
     return _lib
+
+
+class SynthModel(C.Structure):
+    _fields_ = [("n_out", C.c_uint64), ("n_terms", C.c_uint64), ("term_ptr", C.POINTER(C.c_uint64)),
+                ("term_feat", C.POINTER(C.c_uint32)), ("term_coef", C.POINTER(C.c_int32)),
+                ("window_start", C.POINTER(C.c_uint32)), ("window_len", C.POINTER(C.c_uint32))]
+
+
+def synth_model(seed, n_tags, n_targets, neighbours=5, choices=None):
+    """The seeded synthetic model (oracle_synth_model): returns
+    (term_ptr, term_feat, term_coef, window_start, window_len) arrays."""
+    ch = None if not choices else np.ascontiguousarray(choices, np.uint32)
+    m = SynthModel()
+    rc = lib().oracle_synth_model(seed, n_tags, n_targets, 0 if ch is not None else neighbours,
+                                  0 if ch is None else len(ch), _p(ch, C.c_uint32), C.byref(m))
+    if rc != 0:
+        raise ValueError("oracle_synth_model failed")
+    try:
+        arr = np.ctypeslib.as_array
+        out = (arr(m.term_ptr, (m.n_out + 1,)).copy(), arr(m.term_feat, (m.n_terms,)).copy(),
+               arr(m.term_coef, (m.n_terms,)).copy(),
+               arr(m.window_start, (n_targets,)).copy() if n_targets else np.zeros(0, np.uint32),
+               arr(m.window_len, (n_targets,)).copy() if n_targets else np.zeros(0, np.uint32))
+    finally:
+        lib().oracle_synth_model_free(C.byref(m))
+    return out
 
 
 def _p(a, t):

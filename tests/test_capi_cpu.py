@@ -105,3 +105,22 @@ def test_digest_host_restates_the_word_hash(lib, index_base):
     want = int(h.astype(np.uint64).sum(dtype=np.uint64))
     got = lib.idash_digest_host(words.ctypes.data_as(C.POINTER(C.c_uint32)), words.size, index_base)
     assert got == want
+
+
+@pytest.mark.parametrize("spec", [dict(n_tags=200, n_targets=500, neighbours=5),
+                                  dict(n_tags=300, n_targets=800, choices=[5, 10, 20, 30, 50]),
+                                  dict(n_tags=7, n_targets=40, neighbours=10)])
+def test_oracle_restates_the_synthetic_model(oracle, spec):
+    """The benchmark's CPU reference arm builds its workload with the oracle's
+    generator (no product import): it must be the product's model exactly."""
+    from idash2019_2_gb300 import gpu
+    choices = spec.get("choices")
+    w = gpu.synth_model(seed=0x1DA52019, n_tags=spec["n_tags"], n_targets=spec["n_targets"],
+                        neighbours=spec.get("neighbours", 5), choices=choices)
+    ptr, feat, coef, ws, wl = oracle.synth_model(0x1DA52019, spec["n_tags"], spec["n_targets"],
+                                                 neighbours=spec.get("neighbours", 5), choices=choices)
+    np.testing.assert_array_equal(ptr, w.model.term_ptr)
+    np.testing.assert_array_equal(feat, w.model.term_feat)
+    np.testing.assert_array_equal(coef, w.model.term_coef)
+    np.testing.assert_array_equal(ws, w.window_start)
+    np.testing.assert_array_equal(wl, w.window_len)

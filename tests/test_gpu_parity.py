@@ -366,42 +366,3 @@ def test_errors_are_statuses(ctx):
     with pytest.raises(gpu.IdashError):
         m.score_device(d.ptr + 4, gpu.DENSE_TRLWE, d.ptr, gpu.DENSE_TRLWE)  # misaligned payload
     ctx.sync()
-
-
-@pytest.mark.slow
-def test_full_scale_trlwe_checksum_and_samples(ctx, oracle):
-    """80,882 targets x 3 outputs, 16,184 tags, 1,000 individuals (R = 1):
-    column sums of all outputs equal sum_f (sum_o w_of) C_f + biases (mod 2^32),
-    and sampled outputs match the oracle exactly."""
-    w = gpu.synth_model(seed=0x1DA52019, n_tags=16184, n_targets=80882, neighbours=5)
-    params = gpu.TrlweParams(1024, 1, 1000, 1, 1024, 1 << 18, 42)
-    n_rows = 3 * 16184
-    d_in = ctx.device_alloc(n_rows * 8192)
-    gpu.synth_trlwe_device(ctx, 5, params, 16184, d_in.ptr, gpu.DENSE_TRLWE)
-    m = gpu.TrlweModel(ctx, w.model, n_rows, 1000, 1, 1024)
-    d_out = ctx.device_alloc(m.n_out * 8192)
-    m.score_device(d_in.ptr, gpu.DENSE_TRLWE, d_out.ptr, gpu.DENSE_TRLWE)
-    ctx.sync()
-    rows = d_in.download(dtype=np.int32).reshape(n_rows, 2048)
-    out = d_out.download(dtype=np.int32).reshape(m.n_out, 2048)
-    colsum = out.view(np.uint32).sum(axis=0, dtype=np.uint64) & 0xFFFFFFFF
-    csr = w.model
-    wsum = np.zeros(n_rows, np.uint64)
-    bias = np.uint64(0)
-    for o in range(csr.n_out):
-        for t in range(int(csr.term_ptr[o]), int(csr.term_ptr[o + 1])):
-            f, c = int(csr.term_feat[t]), int(csr.term_coef[t]) & 0xFFFFFFFF
-            if f == 0xFFFFFFFF:
-                bias = (bias + np.uint64(c * (1 << 18))) & np.uint64(0xFFFFFFFF)
-            else:
-                wsum[f] = (wsum[f] + np.uint64(c)) & np.uint64(0xFFFFFFFF)
-    want = np.zeros(2048, np.uint64)
-    r32 = rows.view(np.uint32).astype(np.uint64)
-    for f in np.nonzero(wsum)[0]:
-        want = (want + wsum[f] * r32[f]) & np.uint64(0xFFFFFFFF)
-    want[1024:1024 + 1000] = (want[1024:1024 + 1000] + bias) & np.uint64(0xFFFFFFFF)
-    np.testing.assert_array_equal(colsum, want)
-    for lo in (0, 120003, csr.n_out - 60):
-        sub = csr.slice_outputs(lo, lo + 60)
-        got_o, _ = oracle.trlwe_score(sub.term_ptr, sub.term_feat, sub.term_coef, rows, 1000, 1, 1024)
-        np.testing.assert_array_equal(out[lo:lo + 60], got_o)

@@ -112,9 +112,10 @@ def test_the_mix_overlaps_requests(served):
     assert all(r["done_s"] >= r["admit_s"] - 1e-3 for r in res)
 
 
-def test_served_outputs_match_the_oracle(served, oracle):
+def test_every_served_request_matches_the_oracle(served, oracle):
+    """Every request of the mix, every individual block, word for word."""
     ctx, w, m, reqs, res, outs = served
-    for i in (1, 6):
+    for i in range(len(reqs)):
         r = reqs[i]
         o0, o1 = 3 * r["target_begin"], 3 * r["target_end"]
         lo, hi = m.input_rows(o0, o1)
