@@ -39,6 +39,9 @@ WORKLOADS = {
     "trlwe_full": dict(n_indiv=1000, n_tags=16184, n_targets=80882, neighbours=5,
                        desc="full scale, TRLWE-packed (reference layout): 1,000 individuals, 16,184 tags, "
                             "80,882 targets x 3 outputs, 5 neighbours, N=1024, NUM_REGIONS=1"),
+    "trlwe_prof": dict(n_indiv=1000, n_tags=8000, n_targets=40000, neighbours=5,
+                       desc="profiling size, TRLWE-packed: 1,000 individuals, 8,000 tags, 40,000 targets x 3 outputs, "
+                            "5 neighbours, NUM_REGIONS=1 (inputs 197 MB > L2)"),
     "trlwe_r10": dict(n_indiv=100, n_tags=500, n_targets=2000, neighbours=5,
                       desc="CPU-runnable size, TRLWE-packed: 100 individuals (NUM_REGIONS=10, REGION_SIZE=102), "
                            "500 tags, 2,000 targets x 3 outputs, 5 neighbours"),
@@ -51,7 +54,9 @@ UNIT = "predictions/s"
 PUBLISHED_PREDICTIONS_PER_S = 1004 * 80882 * 3 / 3.06433
 KERNEL_NAMES = {0: "window (batched, persistent, CUDA graph)", 1: "direct (plain)",
                 2: "pipe (batched, double-buffered, persistent, CUDA graph)",
-                3: "ws (batched, warp-specialised producer + consumers over an mbarrier ring, CUDA graph)"}
+                3: "ws (batched, warp-specialised producer + consumers over an mbarrier ring, CUDA graph)",
+                4: "tc (batched, tensor cores: exact fp16 digit products on tcgen05.mma, fp32 accumulators in TMEM, "
+                   "CUDA graph)"}
 
 
 class timed_range:
@@ -258,7 +263,7 @@ def section_kinds(ctx, w, spec, d_in, d_out, steps):
     from idash2019_2_gb300 import gpu
     out = {}
     lay = gpu.DENSE_TRLWE
-    for option, name in ((2, "window"), (3, "pipe"), (4, "ws")):
+    for option, name in ((2, "window"), (3, "pipe"), (4, "ws"), (5, "tc")):
         ctx.set_option("kernel", option)
         try:
             m = gpu.TrlweModel(ctx, w.model, spec["n_rows"], spec["num_samples"], spec["regions"],
@@ -587,6 +592,8 @@ def run_ours(args):
     ctx = gpu.Context(local)
     w = gpu.synth_model(args.seed + rank, spec["n_tags"], spec["n_targets"], neighbours=spec["neighbours"])
     params = gpu.TrlweParams(1024, 1, spec["num_samples"], spec["regions"], spec["region_size"], 1 << 18, 42)
+    if args.kernel is not None:
+        ctx.set_option("kernel", args.kernel)
     model = gpu.TrlweModel(ctx, w.model, spec["n_rows"], spec["num_samples"], spec["regions"], spec["region_size"])
     d_in = ctx.device_alloc(spec["n_rows"] * 8192)
     d_out = ctx.device_alloc(model.n_out * 8192)
@@ -717,6 +724,8 @@ def main():
     ap.add_argument("--no-headline", action="store_true",
                     help="measure only --sections (no headline, e2e or CPU baseline)")
     ap.add_argument("--small", action="store_true", help="LWE sections at a reduced size (profiling)")
+    ap.add_argument("--kernel", type=int, default=None,
+                    help="the headline model's kernel option (idash_set_option 'kernel'; default: autotuned)")
     args = ap.parse_args()
     args.steps_given = args.steps is not None
     if args.steps is None:

@@ -33,6 +33,7 @@ NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O3"
 
 LIB_SOURCES = [
     "csrc/score_kernels.cu",
+    "csrc/score_tc.cu",
     "csrc/synth.cu",
     "csrc/noalloc.cu",
     "csrc/noalloc_plan.cpp",

@@ -106,6 +106,13 @@ BuiltPlan make_plan(const idash_model *m, const Candidate &c) {
     } else {
         in.one_t32 = m->lp.one_t32;
     }
+    BuiltPlan b;
+    if (c.kind == KernelKind::kTc) {
+        TcLimits tl;
+        tl.max_k = c.slots;
+        b.err = build_tc_plan(in, tl, &b.plan, &b.index_error);
+        return b;
+    }
     PlanLimits lim;
     lim.group_size = c.g;
     lim.max_slots = c.slots;
@@ -114,7 +121,6 @@ BuiltPlan make_plan(const idash_model *m, const Candidate &c) {
     // batched kinds split neighbourhoods larger than one window into parts
     // (later launches accumulate); the direct kernel reads global memory
     lim.split = c.split && c.kind != KernelKind::kDirect;
-    BuiltPlan b;
     b.err = build_plan(in, lim, &b.plan, &b.index_error);
     if (b.err.empty() && (b.plan.blocks.size() >= 0xFFFFFFFFull || b.plan.terms.size() >= 0xFFFFFFFFull))
         b.err = "model too large for 32-bit plan indices";
@@ -133,6 +139,10 @@ idash_status upload_plan(idash_model *m, const Candidate &c, BuiltPlan &&b) {
     if ((s = upload(ctx, &m->d_slots, plan.slots)) != IDASH_OK) return s;
     if ((s = upload(ctx, &m->d_groups, plan.groups)) != IDASH_OK) return s;
     if ((s = upload(ctx, &m->d_terms, plan.terms)) != IDASH_OK) return s;
+    if (c.kind == KernelKind::kTc) {
+        if ((s = upload(ctx, &m->d_tc_a, plan.tc_a)) != IDASH_OK) return s;
+        if ((s = upload(ctx, &m->d_tc_bias, plan.tc_bias)) != IDASH_OK) return s;
+    }
     if (m->form == Form::kTrlwe) {
         if ((s = upload(ctx, &m->d_var_ptr, plan.var_ptr)) != IDASH_OK) return s;
         if ((s = upload(ctx, &m->d_var_row, plan.var_row)) != IDASH_OK) return s;
@@ -149,7 +159,11 @@ idash_status upload_plan(idash_model *m, const Candidate &c, BuiltPlan &&b) {
     m->max_terms = m->plan.max_block_terms;
     m->max_groups = m->plan.max_block_groups;
     uint32_t cps = c.cps;
-    if (c.kind != KernelKind::kDirect) {
+    if (c.kind == KernelKind::kTc) {
+        if (tc_smem_bytes(m->max_terms) > ctx->smem_optin)
+            return ctx->fail(IDASH_ERR_UNSUPPORTED, "tensor-core plan needs more shared memory than a CTA has");
+        cps = 1;  // one CTA per SM: it owns the SM's tensor memory
+    } else if (c.kind != KernelKind::kDirect) {
         const size_t smem = kernel_smem_bytes(c.kind, c.w, m->max_slots, m->max_terms, m->max_groups, c.stages);
         const int occ = resident_ctas_per_sm(c.kind, c.w, c.g, smem);
         if (occ <= 0) return ctx->fail(IDASH_ERR_CUDA, "scoring kernel cannot be resident with this shared memory");
@@ -197,14 +211,31 @@ ScoreArgs make_args(idash_model *m, const uint8_t *in_payload, uint64_t in_strid
     a.n_stages = m->n_stages;
     a.tile_counter = m->ctx->counter();
     a.err = m->ctx->d_err;
+    if (m->kind == KernelKind::kTc) {
+        // work units of whole column-slice runs of one block, about 32 per
+        // CTA so the persistent grid balances; the block's coefficient digits
+        // are loaded once per unit
+        a.tc_a = m->d_tc_a;
+        a.tc_bias = m->d_tc_bias;
+        a.tc_a_max_bytes = uint32_t(tc_a_bytes(m->max_terms));
+        const uint64_t tiles = uint64_t(a.n_blocks) * a.n_slices;
+        const uint64_t want = std::max<uint64_t>(1, uint64_t(m->ctas) * 32);
+        a.unit_slices = uint32_t(std::min<uint64_t>(a.n_slices, std::max<uint64_t>(1, (tiles + want - 1) / want)));
+        a.units_per_block = (a.n_slices + a.unit_slices - 1) / a.unit_slices;
+        a.n_units = a.n_blocks * a.units_per_block;
+    }
     return a;
 }
 
 idash_status launch(idash_model *m, const ScoreArgs &a, cudaStream_t s) {
     if (uint64_t(a.n_blocks) * a.n_slices >= 0xFFFFFFFFull)
         return m->ctx->fail(IDASH_ERR_UNSUPPORTED, "too many tiles in one launch; score a smaller output range");
-    idash_status st = m->ctx->check_cuda(launch_score(m->kind, m->slice_words, m->group_size, a, m->ctas, s),
-                                         "scoring kernel launch");
+    if (m->kind == KernelKind::kTc && uint64_t(a.n_blocks) * a.units_per_block >= 0xFFFFFFFFull)
+        return m->ctx->fail(IDASH_ERR_UNSUPPORTED, "too many work units in one launch; score a smaller output range");
+    const cudaError_t e = m->kind == KernelKind::kTc
+                              ? launch_score_tc(a, m->ctas, s)
+                              : launch_score(m->kind, m->slice_words, m->group_size, a, m->ctas, s);
+    idash_status st = m->ctx->check_cuda(e, "scoring kernel launch");
     if (st == IDASH_OK && a.n_tiles) m->ctx->stats.kernel_launches++;
     return st;
 }
@@ -331,6 +362,14 @@ std::vector<Candidate> candidates(idash_model *m) {
     std::vector<uint32_t> cpss;
     if (ctx->opt_ctas_per_sm > 0) cpss.push_back(uint32_t(ctx->opt_ctas_per_sm));
     else cpss = {1, 2};
+    // the tensor-core kernel first: exact digit products on tcgen05 (TRLWE
+    // with NUM_REGIONS = 1, and the LWE form), 64-column slices, K up to 192
+    if ((ctx->opt_kernel == 0 || ctx->opt_kernel == 5) && (ctx->opt_slice_words == 0 || ctx->opt_slice_words == 64) &&
+        (m->form == Form::kLwe || (m->form == Form::kTrlwe && m->tp.num_regions == 1))) {
+        Candidate c{KernelKind::kTc, kTcSliceWords, 1, 192, 0, 0, 1};
+        out.push_back(c);
+    }
+    if (ctx->opt_kernel == 5) return out;
     const bool window = ctx->opt_kernel == 0 || ctx->opt_kernel == 2;
     const bool pipe = ctx->opt_kernel == 0 || ctx->opt_kernel == 3;
     const bool use_ws = ctx->opt_kernel == 0 || ctx->opt_kernel == 4;
@@ -350,6 +389,7 @@ std::vector<Candidate> candidates(idash_model *m) {
         const size_t n = out.size();
         for (size_t i = 0; i < n; ++i) {
             Candidate c = out[i];
+            if (c.kind == KernelKind::kTc) continue;
             c.split = true;
             out.push_back(c);
         }
@@ -468,6 +508,10 @@ void idash_model::free_device() {
     cudaFree(d_var_coef);
     cudaFree(d_out_index);
     cudaFree(d_out_row);
+    cudaFree(d_tc_a);
+    cudaFree(d_tc_bias);
+    d_tc_a = nullptr;
+    d_tc_bias = nullptr;
     d_out_row = nullptr;
     d_blocks = nullptr;
     d_slots = nullptr;
@@ -525,6 +569,7 @@ idash_status idash_open(idash_ctx **out, int device) {
         s = ctx->check_cuda(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking), "cudaStreamCreate");
     }
     if (s == IDASH_OK) s = ctx->check_cuda(configure_window_kernels(ctx->smem_optin), "configure kernels");
+    if (s == IDASH_OK) s = ctx->check_cuda(configure_tc_kernel(ctx->smem_optin), "configure tensor-core kernel");
     if (s == IDASH_OK) s = ctx->check_cuda(cudaStreamCreateWithFlags(&ctx->h2d, cudaStreamNonBlocking), "cudaStreamCreate");
     if (s == IDASH_OK) s = ctx->check_cuda(cudaStreamCreateWithFlags(&ctx->d2h, cudaStreamNonBlocking), "cudaStreamCreate");
     if (s == IDASH_OK) s = ctx->check_cuda(cudaEventCreateWithFlags(&ctx->join_in, cudaEventDisableTiming), "cudaEventCreate");
@@ -582,11 +627,12 @@ idash_status idash_set_option(idash_ctx *ctx, const char *name, int64_t value) {
     if (!ctx || !name) return IDASH_ERR_INVALID_ARGUMENT;
     const std::string n(name);
     if (n == "kernel") {
-        if (value < 0 || value > 4) return ctx->fail(IDASH_ERR_INVALID_ARGUMENT, "kernel must be 0 .. 4");
+        if (value < 0 || value > 5) return ctx->fail(IDASH_ERR_INVALID_ARGUMENT, "kernel must be 0 .. 5");
         ctx->opt_kernel = value;
     } else if (n == "slice_words") {
-        if (value != 0 && !slice_supported(uint32_t(value)))
-            return ctx->fail(IDASH_ERR_INVALID_ARGUMENT, "slice_words must be 0, 128, 256, 512, 1024 or 2048");
+        if (value != 0 && value != int64_t(kTcSliceWords) && !slice_supported(uint32_t(value)))
+            return ctx->fail(IDASH_ERR_INVALID_ARGUMENT,
+                             "slice_words must be 0, 64 (tensor-core kernel), 128, 256, 512, 1024 or 2048");
         ctx->opt_slice_words = value;
     } else if (n == "ctas_per_sm") {
         if (value < 0 || value > 8) return ctx->fail(IDASH_ERR_INVALID_ARGUMENT, "ctas_per_sm must be in [0, 8]");

@@ -66,7 +66,7 @@ struct idash_ctx {
     uint32_t next_counter = 0;
 
     // options
-    int64_t opt_kernel = 0;        // 0 window (batched), 1 direct (plain)
+    int64_t opt_kernel = 0;        // 0 autotuned, 1 direct (plain), 2 window, 3 pipe, 4 ws, 5 tensor cores
     int64_t opt_slice_words = 0;   // 0 = autotune
     int64_t opt_ctas_per_sm = 0;   // 0 = autotune / occupancy
     int64_t opt_graph = 1;
@@ -126,6 +126,8 @@ struct idash_model {
     int32_t *d_var_coef = nullptr;
     uint32_t *d_out_index = nullptr;
     uint32_t *d_out_row = nullptr;
+    uint8_t *d_tc_a = nullptr;      // tensor-core plans: coefficient digits per block
+    uint32_t *d_tc_bias = nullptr;  // tensor-core plans: bias per output
 
     // cached CUDA graph of the last device-path call
     cudaGraphExec_t graph = nullptr;

@@ -424,9 +424,10 @@ Status read_model_cache(FlatModel *flat, uint64_t fp, const std::string &path) {
 
 namespace {
 constexpr char kPlanMagic[8] = {'I', 'D', 'G', 'P', 'L', 'A', 'N', '1'};
-// idash_model_info::kernel (0 window, 1 direct, 2 pipe, 3 warp-specialised)
-// as the "kernel" option's value (2, 1, 3, 4)
-constexpr int64_t kKernelOption[4] = {2, 1, 3, 4};
+// idash_model_info::kernel (0 window, 1 direct, 2 pipe, 3 warp-specialised,
+// 4 tensor cores) as the "kernel" option's value (2, 1, 3, 4, 5)
+constexpr int64_t kKernelOption[5] = {2, 1, 3, 4, 5};
+constexpr uint64_t kMaxKernel = 4;
 }  // namespace
 
 bool apply_cached_plan(idash_ctx *ctx, const std::string &cache_path, const std::string &params_file,
@@ -439,14 +440,14 @@ bool apply_cached_plan(idash_ctx *ctx, const std::string &cache_path, const std:
     const bool ok = std::fread(magic, 1, 8, f) == 8 && std::memcmp(magic, kPlanMagic, 8) == 0 &&
                     std::fread(rec, 8, 3, f) == 3;
     std::fclose(f);
-    if (!ok || rec[0] != fingerprint(params_file, model_dir) || rec[1] > 3) return false;
+    if (!ok || rec[0] != fingerprint(params_file, model_dir) || rec[1] > kMaxKernel) return false;
     return idash_set_option(ctx, "kernel", kKernelOption[rec[1]]) == IDASH_OK &&
            idash_set_option(ctx, "slice_words", int64_t(rec[2])) == IDASH_OK;
 }
 
 void save_plan(const std::string &cache_path, const std::string &params_file, const std::string &model_dir,
                const idash_model_info &plan) {
-    if (cache_path.empty() || plan.kernel > 3 || plan.slice_words == 0) return;
+    if (cache_path.empty() || plan.kernel > kMaxKernel || plan.slice_words == 0) return;
     const std::string path = cache_path + ".plan", tmp = path + ".tmp";
     FILE *f = std::fopen(tmp.c_str(), "wb");
     if (!f) return;

@@ -22,28 +22,22 @@ size_t union_size(const uint64_t *a, size_t na, const uint64_t *b, size_t nb) {
     return n + (na - i) + (nb - j);
 }
 
-}  // namespace
+// Step 1 of both planners: every output as (slot key, coefficient) sorted by
+// key, duplicates summed mod 2^32, zero coefficients dropped, constants
+// folded into the bias; the variance program and the distinct row count go
+// into `plan`.
+struct Normalised {
+    std::vector<uint64_t> nptr, nkey;
+    std::vector<uint32_t> ncoef, bias;
+};
 
-std::string build_plan(const PlanInput &in, const PlanLimits &lim, Plan *plan, bool *index_error) {
-    *index_error = false;
-    *plan = Plan();
-    if (lim.group_size != 1 && lim.group_size != 3) return "group_size must be 1 or 3";
-    if (in.n_out >= kNoOutput) return "too many outputs";
-    if (in.form == Form::kTrlwe) {
-        if (in.num_regions == 0 || in.region_size == 0 ||
-            uint64_t(in.num_regions) * in.region_size > in.N)
-            return "NUM_REGIONS * REGION_SIZE must be in [1, N]";
-    }
+std::string normalise(const PlanInput &in, Plan *plan, Normalised *nm, bool *index_error) {
     const uint64_t n_out = in.n_out;
     plan->n_terms_in = n_out ? in.term_ptr[n_out] - in.term_ptr[0] : 0;
-
-    // 1. Normalise every output: (slot key, coefficient) sorted by key,
-    //    duplicates summed mod 2^32, zero coefficients dropped, constants
-    //    folded into the bias.
-    std::vector<uint64_t> nptr(n_out + 1, 0);
-    std::vector<uint64_t> nkey;
-    std::vector<uint32_t> ncoef;
-    std::vector<uint32_t> bias(n_out, 0);
+    std::vector<uint64_t> &nptr = nm->nptr, &nkey = nm->nkey;
+    std::vector<uint32_t> &ncoef = nm->ncoef, &bias = nm->bias;
+    nptr.assign(n_out + 1, 0);
+    bias.assign(n_out, 0);
     nkey.reserve(plan->n_terms_in);
     ncoef.reserve(plan->n_terms_in);
     std::vector<std::pair<uint64_t, uint32_t>> tmp;
@@ -107,6 +101,32 @@ std::string build_plan(const PlanInput &in, const PlanLimits &lim, Plan *plan, b
         for (uint8_t s : seen) d += s;
         plan->distinct_rows = d;
     }
+
+    return "";
+}
+
+}  // namespace
+
+std::string build_plan(const PlanInput &in, const PlanLimits &lim, Plan *plan, bool *index_error) {
+    *index_error = false;
+    *plan = Plan();
+    if (lim.group_size != 1 && lim.group_size != 3) return "group_size must be 1 or 3";
+    if (in.n_out >= kNoOutput) return "too many outputs";
+    if (in.form == Form::kTrlwe) {
+        if (in.num_regions == 0 || in.region_size == 0 ||
+            uint64_t(in.num_regions) * in.region_size > in.N)
+            return "NUM_REGIONS * REGION_SIZE must be in [1, N]";
+    }
+    const uint64_t n_out = in.n_out;
+
+    // 1. Normalise every output.
+    Normalised nm;
+    {
+        const std::string err = normalise(in, plan, &nm, index_error);
+        if (!err.empty()) return err;
+    }
+    const std::vector<uint64_t> &nptr = nm.nptr, &nkey = nm.nkey;
+    const std::vector<uint32_t> &ncoef = nm.ncoef, &bias = nm.bias;
 
     // 2. Groups of up to group_size consecutive outputs with (nearly) the
     //    same slot set: union no larger than 5/4 of the largest member + 1.
@@ -260,6 +280,123 @@ std::string build_plan(const PlanInput &in, const PlanLimits &lim, Plan *plan, b
             plan->blocks.push_back(b);
             gi = gend;
         }
+    }
+    plan->phase_begin.push_back(uint32_t(plan->blocks.size()));
+    return "";
+}
+
+namespace {
+
+// fp16 bit pattern of a small integer (|v| <= 2048: exact).
+uint16_t half_bits(int32_t v) {
+    if (v == 0) return 0;
+    const uint16_t sign = v < 0 ? 0x8000u : 0u;
+    uint32_t m = uint32_t(v < 0 ? -v : v);
+    int e = 31 - __builtin_clz(m);
+    return uint16_t(sign | uint32_t((e + 15) << 10) | ((m << (10 - e)) & 0x3FFu));
+}
+
+// Byte offset of element (row m, k) of one digit plane in the MMA's
+// no-swizzle K-major layout: 8x8 core matrices of 16-byte rows, K-blocks of 8
+// outermost (2,048 bytes each: 128 rows), then 8-row groups (128 bytes).
+inline uint64_t tc_a_offset(uint32_t m, uint32_t k) {
+    return uint64_t(k / 8) * 2048 + (m / 8) * 128 + (m % 8) * 16 + (k % 8) * 2;
+}
+
+}  // namespace
+
+std::string build_tc_plan(const PlanInput &in, const TcLimits &lim, Plan *plan, bool *index_error) {
+    *index_error = false;
+    *plan = Plan();
+    if (in.n_out >= kNoOutput) return "too many outputs";
+    if (in.form == Form::kIntPoly) return "the tensor-core plan serves the TRLWE and LWE forms";
+    if (in.form == Form::kTrlwe && in.num_regions != 1)
+        return "the tensor-core plan reads rows unrotated (NUM_REGIONS = 1)";
+    const uint64_t n_out = in.n_out;
+    Normalised nm;
+    {
+        const std::string err = normalise(in, plan, &nm, index_error);
+        if (!err.empty()) return err;
+    }
+    // coefficient digits c = c0 + 256 c1, c0 in [-128, 127]; |c1| <= 128
+    int32_t max_c1 = 0;
+    for (uint32_t c : nm.ncoef) {
+        const int32_t c0 = int32_t((c + 128u) & 255u) - 128;
+        const int64_t c1 = (int64_t(int32_t(c)) - c0) / 256;
+        if (c1 < -128 || c1 > 128) return "a coefficient needs more than two base-256 digits";
+        max_c1 = std::max<int32_t>(max_c1, int32_t(c1 < 0 ? -c1 : c1));
+    }
+    const uint64_t per_k = uint64_t(128) * uint64_t(128 + max_c1);
+    uint32_t k_max = uint32_t(((uint64_t(1) << 22) - 1) / per_k) / 16 * 16;
+    k_max = std::min(k_max, lim.max_k / 16 * 16);
+    if (k_max < 16) return "no K satisfies the exactness bound";
+
+    plan->tc_bias.assign(nm.bias.begin(), nm.bias.end());
+    plan->phase_begin.push_back(0);
+    std::vector<uint64_t> win, merged;
+    for (uint64_t o = 0; o < n_out;) {
+        win.clear();
+        uint64_t e = o;
+        while (e < n_out && e - o < kTcRows) {
+            const uint64_t *k0 = nm.nkey.data() + nm.nptr[e], *k1 = nm.nkey.data() + nm.nptr[e + 1];
+            merged.clear();
+            std::set_union(win.begin(), win.end(), k0, k1, std::back_inserter(merged));
+            if (merged.size() > k_max) {
+                if (e == o) return "an output reads more rows than one tensor-core block holds";
+                break;
+            }
+            win.swap(merged);
+            ++e;
+        }
+        for (uint64_t k : win)
+            if ((k & 0xFFFFFFFFu) != 0) return "the tensor-core plan reads rows unrotated";
+        PlanBlock b{};
+        b.slot_begin = uint32_t(plan->slots.size());
+        b.n_slots = uint16_t(win.size());
+        b.n_rot = 0;
+        const uint32_t k_pad = std::max<uint32_t>(16, uint32_t((win.size() + 15) / 16 * 16));
+        b.group_begin = uint32_t(plan->tc_a.size() / 16);
+        b.n_groups = k_pad;
+        b.term_begin = 0;
+        for (size_t c0 = 0, c = 0; c0 < win.size(); c0 += 32, ++c) {
+            const size_t c1 = std::min(win.size(), c0 + 32);
+            bool run = true;
+            for (size_t k = c0 + 1; k < c1 && run; ++k) run = (win[k] >> 32) == (win[c0] >> 32) + (k - c0);
+            if (run && c < 32) b.term_begin |= 1u << c;
+        }
+        b.n_terms = uint32_t(nm.nptr[e] - nm.nptr[o]);
+        b.out_lo = uint32_t(o);
+        b.out_hi = uint32_t(e);
+        uint32_t max_row = 0, min_row = win.empty() ? 0u : 0xFFFFFFFFu;
+        for (uint64_t k : win) {
+            plan->slots.push_back(PlanSlot{uint32_t(k >> 32), 0});
+            max_row = std::max(max_row, uint32_t(k >> 32));
+            min_row = std::min(min_row, uint32_t(k >> 32));
+        }
+        plan->block_max_row.push_back(max_row);
+        plan->block_min_row.push_back(min_row);
+        // the block's coefficient digits: plane 0 holds c0, plane 1 holds c1
+        const size_t a0 = plan->tc_a.size();
+        const uint64_t plane = tc_a_bytes(k_pad) / 2;
+        plan->tc_a.resize(a0 + tc_a_bytes(k_pad), 0);
+        uint8_t *A = plan->tc_a.data() + a0;
+        for (uint64_t p = o; p < e; ++p) {
+            const uint32_t m = uint32_t(p - o);
+            size_t idx = 0;
+            for (uint64_t t = nm.nptr[p]; t < nm.nptr[p + 1]; ++t) {
+                while (win[idx] != nm.nkey[t]) ++idx;
+                const uint32_t c = nm.ncoef[t];
+                const int32_t c0 = int32_t((c + 128u) & 255u) - 128;
+                const int32_t c1 = int32_t((int64_t(int32_t(c)) - c0) / 256);
+                const uint16_t h0 = half_bits(c0), h1 = half_bits(c1);
+                std::memcpy(A + tc_a_offset(m, uint32_t(idx)), &h0, 2);
+                std::memcpy(A + plane + tc_a_offset(m, uint32_t(idx)), &h1, 2);
+            }
+        }
+        plan->max_block_slots = std::max<uint32_t>(plan->max_block_slots, b.n_slots);
+        plan->max_block_terms = std::max(plan->max_block_terms, k_pad);
+        plan->blocks.push_back(b);
+        o = e;
     }
     plan->phase_begin.push_back(uint32_t(plan->blocks.size()));
     return "";

@@ -100,7 +100,36 @@ struct Plan {
     uint32_t max_row_per_block_hint = 0;
     std::vector<uint32_t> block_max_row;  // per block: largest input row read
     std::vector<uint32_t> block_min_row;  // per block: smallest input row read (0 if none)
+    // Tensor-core plans only (build_tc_plan): per block, the coefficient
+    // digits in the MMA's shared-memory layout, and every output's bias.
+    std::vector<uint8_t> tc_a;
+    std::vector<uint32_t> tc_bias;
 };
+
+// Tensor-core plans (build_tc_plan).  A block is up to kTcRows consecutive
+// outputs (the MMA's M, one TMEM lane each) over the sorted union of their
+// input rows (the MMA's K, padded to a multiple of 16).  PlanBlock fields are
+// read as: slot_begin/n_slots the rows, n_rot 0, group_begin the offset of the
+// block's coefficient digits in tc_a in 16-byte units, n_groups the padded K,
+// term_begin a bit mask of the block's 32-row chunks whose rows are
+// consecutive (bit c: rows 32c .. min(32c + 32, n_slots) - 1; such a chunk is
+// one 2D tensor copy), n_terms the block's nonzero terms, out_lo/out_hi its
+// outputs.
+//
+// Exactness (fp16 digits, fp32 accumulation): a ciphertext word x is split
+// into four balanced base-256 digits (x + 0x80808080 byte by byte, minus 128),
+// a coefficient c into c0 in [-128, 127] and c1 = (c - c0) / 256; product
+// digit sums for shift 8s are sums over K of at most two digit products, so
+// |sum| <= K * 128 * (128 + max|c1|).  The planner keeps that below 2^22
+// (where x + 1.5 * 2^23 is exact in fp32) by bounding K, and refuses models
+// with a coefficient outside two digits.
+constexpr uint32_t kTcRows = 128;
+struct TcLimits {
+    uint32_t max_k = 192;  // shared-memory bound on the padded K
+};
+// Bytes of one block's coefficient digits: 2 digit planes x 128 rows x k_pad fp16.
+inline uint64_t tc_a_bytes(uint32_t k_pad) { return uint64_t(4) * kTcRows * k_pad; }
+std::string build_tc_plan(const PlanInput &in, const TcLimits &lim, Plan *plan, bool *index_error);
 
 // Returns "" on success, else a message; *index_error is set when a term
 // names a feature without an input row (IDASH_ERR_INDEX).

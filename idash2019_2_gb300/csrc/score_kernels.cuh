@@ -42,6 +42,17 @@ struct ScoreArgs {
     // written, row r and column c, is added to *digest.
     unsigned long long *digest;
     uint64_t digest_base;         // a multiple of 4
+    // KernelKind::kTc only.  tc_a: per block, the coefficient digits in the
+    // MMA's shared-memory layout (PlanBlock::group_begin is the block's
+    // offset in 16-byte units, PlanBlock::n_groups its padded K); tc_bias:
+    // every output's bias.  Work unit u covers column slices
+    // [(u % units_per_block) * unit_slices, + unit_slices) of block
+    // block_lo + u / units_per_block.
+    const uint8_t *tc_a;
+    const uint32_t *tc_bias;
+    uint32_t unit_slices, units_per_block, n_units;
+    uint32_t tc_a_max_bytes;      // shared-memory room for one block's digits
+    uint32_t tc_use_map;          // set by the launch: consecutive-row chunks come by 2D tensor copy
 };
 
 // kWindow: persistent, 256 threads, one shared-memory buffer, 1-2 CTAs/SM.
@@ -51,7 +62,11 @@ struct ScoreArgs {
 // kWs:     persistent, warp-specialised: one CTA of 1 producer + 15 consumer
 //          warps per SM over a ring of n_stages buffers handed over with
 //          mbarriers; consumers take (group, part) units from a shared counter.
-enum class KernelKind : int { kWindow = 0, kDirect = 1, kPipe = 2, kWs = 3 };
+// kTc:     persistent, tensor cores (tcgen05.mma, fp16 digits, fp32
+//          accumulators in TMEM): one CTA per SM; blocks of up to 128
+//          outputs x 64-column slices (score_tc.cu).
+enum class KernelKind : int { kWindow = 0, kDirect = 1, kPipe = 2, kWs = 3, kTc = 4 };
+constexpr uint32_t kTcSliceWords = 64;  // columns per tensor-core tile (the MMA's N)
 constexpr uint32_t kMaxStages = 4;
 constexpr uint32_t kWsHeaderBytes = 512;  // kWs: barriers + per-stage headers before the ring
 
@@ -104,5 +119,12 @@ struct FinalizeArgs {
     int32_t tag;
 };
 cudaError_t launch_finalize(const FinalizeArgs &a, cudaStream_t stream);
+
+// Tensor-core kernel (score_tc.cu): dynamic shared memory for a plan whose
+// largest padded K is max_k_pad, its launch (grid = ctas, one per SM at
+// most), and the one-off shared-memory attribute.
+size_t tc_smem_bytes(uint32_t max_k_pad);
+cudaError_t launch_score_tc(const ScoreArgs &a, uint32_t ctas, cudaStream_t stream);
+cudaError_t configure_tc_kernel(size_t max_smem);
 
 }  // namespace idash

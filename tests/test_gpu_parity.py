@@ -73,7 +73,7 @@ def test_model_cache_is_written_then_used(tmp_path, monkeypatch):
         raw = plan.read_bytes()
         assert len(raw) == 32 and raw[:8] == b"IDGPLAN1"
         kind, slice_words = np.frombuffer(raw[16:], np.uint64)
-        assert kind <= 3 and slice_words in (128, 256, 512, 1024, 2048)
+        assert (kind <= 3 and slice_words in (128, 256, 512, 1024, 2048)) or (kind == 4 and slice_words == 64)
     # a damaged plan file is ignored and replaced
     plan.write_bytes(b"IDGPLAN1" + b"\xff" * 24)
     rep = gpu.cloud_files(str(tmp_path / "params.bin"), str(tmp_path / "model"),
@@ -267,8 +267,10 @@ def test_trlwe_autotune_picks_a_correct_plan(ctx, oracle):
     np.testing.assert_array_equal(got, want)
     np.testing.assert_array_equal(got2, want)
     info = m.info()
-    # a batched kind (window, pipe or warp-specialised) at a TRLWE slice width
-    assert info["kernel"] in (0, 2, 3) and info["slice_words"] in (512, 1024, 2048)
+    # a batched kind: window, pipe or warp-specialised at a TRLWE slice width,
+    # or the tensor-core kernel at its 64-word slices
+    assert (info["kernel"] in (0, 2, 3) and info["slice_words"] in (512, 1024, 2048)) or \
+        (info["kernel"] == 4 and info["slice_words"] == 64)
 
 
 @pytest.mark.parametrize("kernel,slice_words,split", [(0, 0, 1), (2, 128, 1), (3, 256, 1), (3, 512, 1), (1, 256, 1),
