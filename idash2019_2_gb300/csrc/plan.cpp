@@ -287,13 +287,15 @@ std::string build_plan(const PlanInput &in, const PlanLimits &lim, Plan *plan, b
 
 namespace {
 
-// fp16 bit pattern of a small integer (|v| <= 2048: exact).
+// fp16 bit pattern of an integer that fp16 holds exactly (|v| < 65536 with
+// at most 11 significant bits, e.g. every |v| <= 2048).
 uint16_t half_bits(int32_t v) {
     if (v == 0) return 0;
     const uint16_t sign = v < 0 ? 0x8000u : 0u;
-    uint32_t m = uint32_t(v < 0 ? -v : v);
-    int e = 31 - __builtin_clz(m);
-    return uint16_t(sign | uint32_t((e + 15) << 10) | ((m << (10 - e)) & 0x3FFu));
+    const uint32_t m = uint32_t(v < 0 ? -v : v);
+    const int e = 31 - __builtin_clz(m);
+    const uint32_t frac = e <= 10 ? (m << (10 - e)) : (m >> (e - 10));
+    return uint16_t(sign | uint32_t((e + 15) << 10) | (frac & 0x3FFu));
 }
 
 // Byte offset of element (row m, k) of one digit plane in the MMA's
