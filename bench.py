@@ -9,15 +9,19 @@ TRLWE (N = 1024), 16,184 tag SNPs (48,552 input TRLWE), 80,882 targets x 3
 outputs (242,646 output TRLWE), 5 nearest-tag neighbours, coefficients
 uniform in [-8192, 8191]; synthetic seeded data.
 
-  value   predictions/s with inputs and model resident in HBM (CUDA events
-          on the launching stream; inputs 0.4 GB > L2, outputs 2 GB)
-  e2e     the same through idash_score_trlwe_host with page-locked host
-          buffers: every step copies the inputs in and the outputs out
-  roofline the scoring kernel against the measured HBM copy bandwidth
+  value        predictions/s with inputs and model resident in HBM (CUDA
+               events on the launching stream; inputs 0.4 GB > L2, outputs 2 GB)
+  e2e          the same through idash_score_trlwe_host with page-locked host
+               buffers: every step copies the inputs in and the outputs out
+  roofline     the scoring kernel against the measured HBM copy bandwidth
   cpu_baseline the oracle's restatement of the reference loop on the host cores
+  forms        the other configurations and layouts, each with its own bound
+               and a CPU timing of the oracle beside it (sampled where a full
+               pass is too slow for the host, and labelled so)
 
 --impl reference times that CPU restatement alone (all host threads) on the
-same workload and prints the same line with impl=reference.
+same workload and prints the same line with impl=reference; it builds the
+workload from the oracle alone (no part of the GPU library is loaded).
 Multi-GPU (torchrun): each rank scores its own batch of the same size
 (weak scaling, no collective on the data path); max time over ranks.
 """
@@ -52,11 +56,23 @@ UNIT = "predictions/s"
 # targets x 3 in 3.06433 s of "fhe wall time" on a 4-thread laptop
 # (README.md:220-245), i.e. about 79.5 M predictions/s.
 PUBLISHED_PREDICTIONS_PER_S = 1004 * 80882 * 3 / 3.06433
-KERNEL_NAMES = {0: "window (batched, persistent, CUDA graph)", 1: "direct (plain)",
-                2: "pipe (batched, double-buffered, persistent, CUDA graph)",
-                3: "ws (batched, warp-specialised producer + consumers over an mbarrier ring, CUDA graph)",
-                4: "tc (batched, tensor cores: exact fp16 digit products on tcgen05.mma, fp32 accumulators in TMEM, "
-                   "CUDA graph)"}
+KERNEL_NAMES = {0: "window", 1: "direct (plain)", 2: "pipe", 3: "ws (warp-specialised, IMAD)",
+                4: "tc (tensor cores, exact fp16 digit products)"}
+# 32-bit integer multiply-adds per second measured on this GB300 (one-off
+# throughput probe, profiles/device_limits.txt)
+IMAD_PEAK = 20.07e12
+CONSTANT = 0xFFFFFFFF
+
+
+def sig(x, n=4):
+    """x with floats rounded to n significant digits (recursively)."""
+    if isinstance(x, float):
+        return float(f"{x:.{n}g}")
+    if isinstance(x, dict):
+        return {k: sig(v, n) for k, v in x.items()}
+    if isinstance(x, (list, tuple)):
+        return [sig(v, n) for v in x]
+    return x
 
 
 class timed_range:
@@ -73,11 +89,13 @@ class timed_range:
 
 
 def peaks():
+    """Measured HBM copy bandwidth (GB/s) and dense bf16 tensor rate
+    (TFLOP/s, burst) from MEASURED_PEAKS.json, else the machine's fallback."""
     try:
         p = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
-        return float(p["hbm_gbs"]), "measured"
+        return {"hbm": float(p["hbm_gbs"]), "bf16": float(p["bf16_tflops"]), "source": "measured"}
     except Exception:
-        return 6800.0, "fallback"
+        return {"hbm": 6800.0, "bf16": 1900.0, "source": "fallback"}
 
 
 def profiled_traffic(name: str):
@@ -90,6 +108,35 @@ def profiled_traffic(name: str):
     except OSError:
         pass
     return None
+
+
+def hbm_roofline(alg_bytes, seconds):
+    p = peaks()
+    achieved = alg_bytes / seconds / 1e9
+    return {"bound": "hbm", "achieved": achieved, "peak": p["hbm"], "unit": "GB/s", "frac": achieved / p["hbm"],
+            "peak_source": p["source"]}
+
+
+def compute_roofline(kind, useful_macs, dense_macs, alg_bytes, seconds):
+    """The bound of an accumulate kernel that is not HBM-bound: the IMAD
+    kernels against the measured IMAD rate (useful multiply-adds), the
+    tensor-core kernel against the measured dense fp16/bf16 tensor rate
+    (digit multiply-adds it executes, padding included); the HBM fraction of
+    the algorithmic bytes beside it."""
+    p = peaks()
+    hbm = hbm_roofline(alg_bytes, seconds)
+    if kind == 4:
+        achieved = dense_macs / seconds / 1e12
+        peak = p["bf16"] / 2
+        out = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "T MAC/s", "frac": achieved / peak}
+    else:
+        achieved = useful_macs / seconds / 1e12
+        out = {"bound": "imad", "achieved": achieved, "peak": IMAD_PEAK / 1e12, "unit": "T MAC/s",
+               "frac": achieved / (IMAD_PEAK / 1e12)}
+    out["useful_mac_per_s"] = useful_macs / seconds
+    out["hbm_frac"] = hbm["frac"]
+    out["hbm_achieved_gbs"] = hbm["achieved"]
+    return out
 
 
 class ClockSampler:
@@ -140,6 +187,7 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(sel)}
 
 
+
 def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -160,25 +208,6 @@ def max_over_ranks(x: float) -> float:
     return float(t.item())
 
 
-def cpu_baseline(model_csr, rows, spec, min_seconds=10.0, max_reps=1000):
-    """The oracle's restatement of the reference loop (OpenMP over outputs,
-    eval/idash.cpp:779-842) on all host cores, full workload per rep."""
-    import pyoracle
-    cores = os.cpu_count() or 1
-    preds = spec["n_indiv"] * spec["n_targets"] * 3
-    reps, t0 = 0, time.perf_counter()
-    while True:
-        pyoracle.trlwe_score(model_csr.term_ptr, model_csr.term_feat, model_csr.term_coef, rows, spec["num_samples"],
-                             spec["regions"], spec["region_size"], n_threads=cores)
-        reps += 1
-        el = time.perf_counter() - t0
-        if el >= min_seconds or reps >= max_reps:
-            break
-    return {"value": preds * reps / el, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": f"{reps} full passes of the workload ({el:.1f} s), oracle/oracle.c restatement of "
-                      f"eval/idash.cpp:779-842, OpenMP {cores} threads"}
-
-
 def workload_spec(name):
     spec = dict(WORKLOADS[name])
     regions = max(1, 1024 // spec["n_indiv"])
@@ -187,40 +216,80 @@ def workload_spec(name):
     return spec
 
 
+def config_of(spec, world):
+    """The workload as both arms print it (the same keys and values)."""
+    in_bytes, out_bytes = spec["n_rows"] * 8192, 3 * spec["n_targets"] * 8192
+    return {"workload": spec["desc"], "individuals": spec["n_indiv"], "targets": spec["n_targets"],
+            "tags": spec["n_tags"], "neighbours": spec["neighbours"], "outputs": 3 * spec["n_targets"],
+            "input_rows": spec["n_rows"], "num_regions": spec["regions"], "region_size": spec["region_size"],
+            "l2": f"inputs {in_bytes / 1e9:.2f} GB and outputs {out_bytes / 1e9:.2f} GB vs the 129 MB L2",
+            "parallelism": f"{world} independent batch(es)"}
+
+
+def cores():
+    return os.cpu_count() or 1
+
+
+def repeat_timed(fn, min_seconds, max_reps=1000):
+    """(reps, seconds): fn() run until min_seconds have passed."""
+    reps, t0 = 0, time.perf_counter()
+    while True:
+        fn()
+        reps += 1
+        el = time.perf_counter() - t0
+        if el >= min_seconds or reps >= max_reps:
+            return reps, el
+
+
+def cpu_trlwe(ptr, feat, coef, rows, spec, min_seconds):
+    """The oracle's restatement of the reference loop (OpenMP over outputs,
+    eval/idash.cpp:779-842) on all host cores, full workload per rep."""
+    import pyoracle
+    preds = spec["n_indiv"] * spec["n_targets"] * 3
+    reps, el = repeat_timed(lambda: pyoracle.trlwe_score(ptr, feat, coef, rows, spec["num_samples"], spec["regions"],
+                                                         spec["region_size"], n_threads=cores()), min_seconds)
+    return {"value": preds * reps / el, "unit": UNIT, "cores": cores(), "kind": "port",
+            "sample": f"{reps} full passes ({el:.1f} s), oracle/oracle.c restatement of eval/idash.cpp:779-842, "
+                      f"OpenMP {cores()} threads"}
+
+
 def run_reference(args):
+    """The reference loop on the host cores: the oracle's restatement of
+    eval/idash.cpp:779-842 (the reference binary needs the absent TFHE
+    library).  The workload comes from the oracle's own restatement of the
+    synthetic generator, so nothing of the GPU library is loaded."""
     import numpy as np
-    from idash2019_2_gb300 import gpu
+    import pyoracle
     rank, world, _ = dist_env()
     if rank != 0:
         return
     spec = workload_spec(args.workload)
-    w = gpu.synth_model(args.seed, spec["n_tags"], spec["n_targets"], neighbours=spec["neighbours"])
+    ptr, feat, coef, _, _ = pyoracle.synth_model(args.seed, spec["n_tags"], spec["n_targets"],
+                                                 neighbours=spec["neighbours"])
     rng = np.random.default_rng(args.seed)
     rows = rng.integers(0, 2 ** 32, size=(spec["n_rows"], 2048), dtype=np.uint64).astype(np.uint32).view(np.int32)
-    import pyoracle
     preds = spec["n_indiv"] * spec["n_targets"] * 3
-    cores = os.cpu_count() or 1
+    run = lambda: pyoracle.trlwe_score(ptr, feat, coef, rows, spec["num_samples"], spec["regions"],
+                                       spec["region_size"], n_threads=cores())
     for _ in range(args.warmup):
-        pyoracle.trlwe_score(w.model.term_ptr, w.model.term_feat, w.model.term_coef, rows, spec["num_samples"],
-                             spec["regions"], spec["region_size"], n_threads=cores)
+        run()
     steps = args.steps if args.steps_given else 3
     t0 = time.perf_counter()
     for _ in range(steps):
-        pyoracle.trlwe_score(w.model.term_ptr, w.model.term_feat, w.model.term_coef, rows, spec["num_samples"],
-                             spec["regions"], spec["region_size"], n_threads=cores)
+        run()
     el = time.perf_counter() - t0
     value = preds * steps / el
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": steps, "warmup": args.warmup,
             "ms_per_step": el / steps * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": value / PUBLISHED_PREDICTIONS_PER_S if args.workload == "trlwe_full" else None,
             "dtype": "int32 (Z/2^32)", "data": "synthetic (seeded)", "impl": "reference",
-            "config": {"workload": spec["desc"]},
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+            "config": config_of(spec, world),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores(), "kind": "port",
                              "sample": f"{steps} full passes; oracle/oracle.c restatement of eval/idash.cpp:779-842 "
                                        f"(the reference's TFHE dependency is absent, so its cloud binary cannot be "
                                        f"built on this host)"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-    print(json.dumps(line), flush=True)
+    print(json.dumps(sig(line)), flush=True)
 
 
 def time_on_stream(ctx, fn, steps):
@@ -239,6 +308,13 @@ def time_on_stream(ctx, fn, steps):
     return e0.elapsed_time(e1) / steps
 
 
+def trlwe_alg_bytes(info, n_out):
+    """Each distinct input TRLWE read once, each output TRLWE written once,
+    the model's CSR (4 B feature + 4 B coefficient per term, 4 B bias + 4 B
+    row pointer per output)."""
+    return info["algorithmic_in_rows"] * 8192 + n_out * 8192 + info["n_terms"] * 8 + n_out * 8
+
+
 def section_plain(ctx, w, spec, d_in, d_out, steps):
     """The plain per-output kernel (k_score_direct) on the same workload."""
     from idash2019_2_gb300 import gpu
@@ -249,17 +325,18 @@ def section_plain(ctx, w, spec, d_in, d_out, steps):
         for _ in range(3):
             m.score_device(d_in.ptr, lay, d_out.ptr, lay)
         ms = time_on_stream(ctx, lambda: m.score_device(d_in.ptr, lay, d_out.ptr, lay), steps)
+        info = m.info()
         m.free()
     finally:
         ctx.set_option("kernel", 0)
     preds = spec["n_indiv"] * spec["n_targets"] * 3
-    return {"value": preds / (ms / 1e3), "unit": UNIT, "ms_per_step": ms,
-            "kernel": "direct: one output per team, every input read from global memory"}
+    return {"value": preds / (ms / 1e3), "ms_per_step": ms,
+            "roofline": hbm_roofline(trlwe_alg_bytes(info, 3 * spec["n_targets"]), ms / 1e3)}
 
 
 def section_kinds(ctx, w, spec, d_in, d_out, steps):
     """Each batched kernel kind on the headline workload, autotuned within its
-    kind (slice width, CTAs per SM, ring depth)."""
+    kind (slice width, CTAs per SM, ring depth): ms per pass."""
     from idash2019_2_gb300 import gpu
     out = {}
     lay = gpu.DENSE_TRLWE
@@ -270,14 +347,296 @@ def section_kinds(ctx, w, spec, d_in, d_out, steps):
                                spec["region_size"])
             for _ in range(3):
                 m.score_device(d_in.ptr, lay, d_out.ptr, lay)
-            ms = time_on_stream(ctx, lambda: m.score_device(d_in.ptr, lay, d_out.ptr, lay), steps)
-            info = m.info()
-            out[name] = {"ms_per_step": ms, "slice_words": info["slice_words"], "n_blocks": info["n_blocks"],
-                         "max_window_slots": info["max_window_slots"]}
+            out[name] = time_on_stream(ctx, lambda: m.score_device(d_in.ptr, lay, d_out.ptr, lay), steps)
             m.free()
         finally:
             ctx.set_option("kernel", 0)
     return out
+
+
+def copy_d2h(ctx, host_ptr, dev_ptr, nbytes):
+    import ctypes as C
+    ctx.check(ctx.lib.idash_copy_d2h(ctx.h, C.c_void_p(host_ptr), C.c_void_p(dev_ptr), nbytes))
+
+
+def copy_h2d(ctx, dev_ptr, host_ptr, nbytes):
+    import ctypes as C
+    ctx.check(ctx.lib.idash_copy_h2d(ctx.h, C.c_void_p(dev_ptr), C.c_void_p(host_ptr), nbytes))
+
+
+def section_config1(ctx, seed):
+    """Configuration 1 (100 individuals, 500 tags, 2,000 targets x 3, 5
+    neighbours) in both layouts: TRLWE-packed as the reference packs 100
+    individuals (NUM_REGIONS 10, REGION_SIZE 102) and per-individual LWE
+    (n = 1024).  Each: device-resident value, e2e from page-locked host
+    buffers (inputs copied in and outputs copied out every step), roofline,
+    and the oracle on all host cores over the whole workload."""
+    import numpy as np
+    import pyoracle
+    from idash2019_2_gb300 import gpu
+    out = {}
+    spec = workload_spec("trlwe_r10")
+    preds = spec["n_indiv"] * spec["n_targets"] * 3
+    w = gpu.synth_model(seed, spec["n_tags"], spec["n_targets"], neighbours=5)
+    csr = w.model
+    # TRLWE-packed
+    params = gpu.TrlweParams(1024, 1, spec["num_samples"], spec["regions"], spec["region_size"], 1 << 18, 42)
+    m = gpu.TrlweModel(ctx, csr, spec["n_rows"], spec["num_samples"], spec["regions"], spec["region_size"])
+    d_in, d_out = ctx.device_alloc(spec["n_rows"] * 8192), ctx.device_alloc(csr.n_out * 8192)
+    gpu.synth_trlwe_device(ctx, seed, params, spec["n_tags"], d_in.ptr, gpu.DENSE_TRLWE)
+    lay = gpu.DENSE_TRLWE
+    run = lambda: m.score_device(d_in.ptr, lay, d_out.ptr, lay)
+    for _ in range(3):
+        run()
+    ms = time_on_stream(ctx, run, 200)
+    info = m.info()
+    h_in, h_out = ctx.host_alloc(spec["n_rows"] * 8192), ctx.host_alloc(csr.n_out * 8192)
+    h_in.array[:] = d_in.download()
+    m.score_host(h_in.ptr, lay, spec["n_rows"], h_out.ptr, lay)
+    reps, el = repeat_timed(lambda: m.score_host(h_in.ptr, lay, spec["n_rows"], h_out.ptr, lay), 0.5)
+    rows = np.frombuffer(h_in.array, np.int32).reshape(spec["n_rows"], 2048).copy()
+    out["trlwe"] = {"value": preds / (ms / 1e3), "ms_per_step": ms, "kernel": KERNEL_NAMES.get(info["kernel"]),
+                    "roofline": hbm_roofline(trlwe_alg_bytes(info, csr.n_out), ms / 1e3),
+                    "e2e": {"value": preds * reps / el, "unit": UNIT, "ms_per_step": el / reps * 1e3,
+                            "h2d_bytes_per_step": spec["n_rows"] * 8192, "d2h_bytes_per_step": csr.n_out * 8192},
+                    "cpu_baseline": cpu_trlwe(csr.term_ptr, csr.term_feat, csr.term_coef, rows, spec, 3.0)}
+    for b in (d_in, d_out, h_in, h_out):
+        b.free()
+    m.free()
+    # per-individual LWE
+    n_indiv, n = 100, 1024
+    n_feat = 3 * spec["n_tags"]
+    stride = gpu.lwe_row_words(n_indiv, n)
+    L = n_indiv * (n + 1)
+    lm = gpu.LweModel(ctx, csr, n_feat, n_indiv, n)
+    d_in, d_out = ctx.device_alloc(n_feat * stride * 4), ctx.device_alloc(csr.n_out * stride * 4)
+    gpu.synth_lwe_device(ctx, seed, n, n_indiv, n_feat, d_in.ptr, stride)
+    run = lambda: lm.score_device(n_indiv, d_in.ptr, stride, 0, csr.n_out, d_out.ptr, stride)
+    run()
+    ms = time_on_stream(ctx, run, 10)
+    info = lm.info()
+    h_in, h_out = ctx.host_alloc(n_feat * stride * 4), ctx.host_alloc(csr.n_out * stride * 4)
+    h_in.array[:] = d_in.download()
+
+    def e2e_step():
+        copy_h2d(ctx, d_in.ptr, h_in.ptr, n_feat * stride * 4)
+        run()
+        copy_d2h(ctx, h_out.ptr, d_out.ptr, csr.n_out * stride * 4)
+
+    e2e_step()
+    reps, el = repeat_timed(e2e_step, 0.5)
+    rows = np.frombuffer(h_in.array, np.int32).reshape(n_feat, stride).copy()
+    creps, cel = repeat_timed(lambda: pyoracle.lwe_score(csr.term_ptr, csr.term_feat, csr.term_coef, rows, n_indiv,
+                                                         0, csr.n_out, n=n, n_threads=cores()), 3.0, 20)
+    alg = info["algorithmic_in_rows"] * L * 4 + csr.n_out * L * 4 + info["n_terms"] * 8 + csr.n_out * 8
+    useful = float(np.count_nonzero(csr.term_feat != CONSTANT)) * L
+    dense = 7.0 * 128 * info["dense_k"] * L
+    out["lwe"] = {"value": preds / (ms / 1e3), "ms_per_step": ms, "kernel": KERNEL_NAMES.get(info["kernel"]),
+                  "roofline": hbm_roofline(alg, ms / 1e3),
+                  "compute": compute_roofline(info["kernel"], useful, dense, alg, ms / 1e3),
+                  "e2e": {"value": preds * reps / el, "unit": UNIT, "ms_per_step": el / reps * 1e3,
+                          "h2d_bytes_per_step": n_feat * stride * 4, "d2h_bytes_per_step": csr.n_out * stride * 4},
+                  "cpu_baseline": {"value": preds * creps / cel, "unit": UNIT, "cores": cores(), "kind": "port",
+                                   "sample": f"{creps} full passes ({cel:.1f} s), oracle LWE restatement, "
+                                             f"OpenMP {cores()} threads"}}
+    for b in (d_in, d_out, h_in, h_out):
+        b.free()
+    lm.free()
+    return out
+
+
+def section_lwe(ctx, seed, n_indiv, n_tags, n_targets, neighbours=5, choices=None, passes=2, chunk=2048,
+                cpu_outputs=48):
+    """Per-individual LWE form: inputs resident (n_indiv LWE samples of n=1024
+    per feature row), outputs produced range by range into a 2-slot HBM ring
+    (the full output does not fit in HBM).  The CPU baseline times the oracle
+    on cpu_outputs outputs spread over the model (their input rows copied
+    back from the device) and scales to predictions/s."""
+    import numpy as np
+    import pyoracle
+    from idash2019_2_gb300 import gpu
+    w = gpu.synth_model(seed, n_tags, n_targets, neighbours=neighbours, choices=choices)
+    csr = w.model
+    n_feat = 3 * n_tags
+    stride = gpu.lwe_row_words(n_indiv)
+    L = n_indiv * 1025
+    d_in = ctx.device_alloc(n_feat * stride * 4)
+    gpu.synth_lwe_device(ctx, seed, 1024, n_indiv, n_feat, d_in.ptr, stride)
+    m = gpu.LweModel(ctx, csr, n_feat, n_indiv)
+    ring = [ctx.device_alloc(chunk * stride * 4) for _ in range(2)]
+    ranges = [(lo, min(lo + chunk, m.n_out)) for lo in range(0, m.n_out, chunk)]
+
+    def one_pass():
+        for c, (lo, hi) in enumerate(ranges):
+            m.score_device(n_indiv, d_in.ptr, stride, lo, hi, ring[c % 2].ptr, stride)
+
+    t0 = time.perf_counter()
+    one_pass()  # the first call autotunes
+    ctx.sync()
+    first_s = time.perf_counter() - t0
+    launches0 = ctx.stats()["kernel_launches"]
+    ms = time_on_stream(ctx, one_pass, passes)
+    launches = (ctx.stats()["kernel_launches"] - launches0) // passes
+    info = m.info()
+    preds = n_indiv * n_targets * 3
+    alg = info["algorithmic_in_rows"] * L * 4 + m.n_out * L * 4 + info["n_terms"] * 8 + m.n_out * 8
+    useful = float(np.count_nonzero(csr.term_feat != CONSTANT)) * L
+    dense = 7.0 * 128 * info["dense_k"] * L
+    # CPU baseline on a sample: 4 runs of cpu_outputs / 4 outputs
+    spent, done = 0.0, 0
+    for lo in np.linspace(0, m.n_out - cpu_outputs // 4, 4).astype(int):
+        hi = int(lo) + cpu_outputs // 4
+        a, b = int(csr.term_ptr[lo]), int(csr.term_ptr[hi])
+        f = csr.term_feat[a:b]
+        real = f != CONSTANT
+        f0, f1 = int(f[real].min()), int(f[real].max()) + 1
+        rows = d_in.download(nbytes=(f1 - f0) * stride * 4, offset=f0 * stride * 4, dtype=np.int32).reshape(f1 - f0,
+                                                                                                          stride)
+        feat = f.copy()
+        feat[real] -= f0
+        ptr = (csr.term_ptr[lo:hi + 1] - a).astype(np.uint64)
+        t1 = time.perf_counter()
+        pyoracle.lwe_score(ptr, feat, csr.term_coef[a:b], rows, n_indiv, 0, hi - lo, n_threads=cores())
+        spent += time.perf_counter() - t1
+        done += hi - lo
+    out = {"value": preds / (ms / 1e3), "ms_per_step": ms, "kernel": KERNEL_NAMES.get(info["kernel"]),
+           "slice_words": info["slice_words"], "launches_per_step": launches, "first_pass_s": first_s,
+           "roofline": compute_roofline(info["kernel"], useful, dense, alg, ms / 1e3),
+           "cpu_baseline": {"value": done * n_indiv / spent, "unit": UNIT, "cores": cores(), "kind": "port",
+                            "sample": f"{done} of {m.n_out} outputs in 4 ranges, {spent:.1f} s, oracle LWE "
+                                      f"restatement, scaled to predictions/s"}}
+    for b in ring:
+        b.free()
+    d_in.free()
+    m.free()
+    return out
+
+
+def section_intpoly(ctx, seed, passes=5, scale=1, cpu_outputs=24):
+    """Integer-polynomial x TRLWE product at full scale: 48,552 input TRLWE
+    (16,184 tags x 3), 242,646 outputs (80,882 targets x 3), 20 neighbours
+    (60 dense int16 weight polynomials per output, |w| <= 8192), one block of
+    1,024 individuals per TRLWE.  Exact (two-prime NTT + CRT).  scale > 1
+    divides the tag and target counts (profiling size).  The CPU baseline is
+    the oracle's schoolbook product on cpu_outputs outputs, scaled."""
+    import numpy as np
+    import pyoracle
+    from idash2019_2_gb300 import gpu
+    n_tags, n_targets = 16184 // scale, 80882 // scale
+    w = gpu.synth_model(seed, n_tags, n_targets, neighbours=20)
+    csr = w.model
+    const = csr.term_feat == CONSTANT
+    owner = np.repeat(np.arange(csr.n_out), np.diff(csr.term_ptr.astype(np.int64)))
+    counts = np.bincount(owner[~const], minlength=csr.n_out)
+    ptr = np.concatenate([[0], np.cumsum(counts)]).astype(np.uint64)
+    feat = csr.term_feat[~const]
+    bias = np.zeros(csr.n_out, np.int32)
+    bias[owner[const]] = csr.term_coef[const]
+    icsr = gpu.CSRModel(ptr, feat, np.zeros(len(feat), np.int32))
+    n_terms, n_rows = len(feat), 3 * n_tags
+    d_poly = ctx.device_alloc(n_terms * 1024 * 2)
+    gpu.synth_int16_device(ctx, seed, n_terms * 1024, 8192, d_poly.ptr)
+    t0 = time.perf_counter()
+    m = gpu.IntpolyModel(ctx, icsr, d_poly.ptr, n_rows, 1024, 1024, bias=bias, poly_on_device=True)
+    build_s = time.perf_counter() - t0
+    polys = d_poly.download(nbytes=int(ptr[cpu_outputs]) * 2048, dtype=np.int16).reshape(-1, 1024)
+    d_poly.free()
+    params = gpu.TrlweParams(1024, 1, 1024, 1, 1024, 1 << 18, 42)
+    d_in = ctx.device_alloc(n_rows * 8192)
+    gpu.synth_trlwe_device(ctx, seed, params, n_tags, d_in.ptr, gpu.DENSE_TRLWE)
+    d_out = ctx.device_alloc(csr.n_out * 8192)
+    run = lambda: m.score_device(d_in.ptr, gpu.DENSE_TRLWE, 0, csr.n_out, d_out.ptr, gpu.DENSE_TRLWE)
+    run()
+    ms = time_on_stream(ctx, run, passes)
+    rows = d_in.download(dtype=np.int32).reshape(n_rows, 2048)
+    t1 = time.perf_counter()
+    pyoracle.intpoly_score(ptr[:cpu_outputs + 1], feat[:int(ptr[cpu_outputs])], polys, bias[:cpu_outputs], rows,
+                           1024, 1024, 0, cpu_outputs, n_threads=cores())
+    cpu_s = time.perf_counter() - t1
+    # The configuration's own algorithmic bytes: int16 weights (2 KiB per
+    # term), input rows in, output rows out.  This implementation keeps the
+    # weights resident NTT-transformed (2 primes x 1,024 words = 8 KiB per
+    # term) and also writes and reads the inputs' transforms: its own
+    # compulsory bytes are larger by the ratio below.
+    alg = n_terms * 1024 * 2 + n_rows * 8192 + csr.n_out * 8192
+    traffic = n_terms * 2 * 1024 * 4 + n_rows * 8192 + 2 * n_rows * 4 * 1024 * 4 + csr.n_out * 8192
+    out = {"value": csr.n_out * 1024 / (ms / 1e3), "ms_per_step": ms, "outputs_per_s": csr.n_out / (ms / 1e3),
+           "terms": n_terms, "model_build_s": build_s,
+           "schoolbook_mac_per_s": n_terms * 2 * 1024 * 1024 / (ms / 1e3),
+           "roofline": hbm_roofline(alg, ms / 1e3),
+           "representation": {"bytes_per_step": traffic, "over_config_bytes": traffic / alg,
+                              "frac": hbm_roofline(traffic, ms / 1e3)["frac"]},
+           "cpu_baseline": {"value": cpu_outputs * 1024 / cpu_s, "unit": UNIT, "cores": cores(), "kind": "port",
+                            "sample": f"{cpu_outputs} of {csr.n_out} outputs ({cpu_s:.1f} s), oracle schoolbook "
+                                      f"negacyclic product, scaled to predictions/s"}}
+    for b in (d_in, d_out):
+        b.free()
+    m.free()
+    return out
+
+
+def section_serving(ctx, seed, n_requests=10000, budget=150 << 30, inflight=4, cpu_requests=6):
+    """Continuous batching (idash_serve_trlwe) over a Poisson stream: each
+    request has individuals ~ U[1, 2000] and a contiguous target range of
+    length ~ U[1000, 80882]; 10 neighbours; model and index tables resident;
+    150 GB HBM admission budget.  The arrival rate is 0.8 x the measured
+    capacity (64 requests arriving at once)."""
+    import numpy as np
+    import pyoracle
+    from idash2019_2_gb300 import gpu
+    T = 80882
+    w = gpu.synth_model(seed, 16184, T, neighbours=10)
+    m = gpu.TrlweModel(ctx, w.model, 3 * 16184, 1024, 1, 1024)
+    rng = np.random.default_rng(seed)
+
+    def draw(k):
+        out = []
+        for i in range(k):
+            length = int(rng.integers(1000, T + 1))
+            t0 = int(rng.integers(0, T - length + 1))
+            out.append(dict(arrival_s=0.0, n_indiv=int(rng.integers(1, 2001)), target_begin=t0,
+                            target_end=t0 + length, seed=int(rng.integers(1, 2 ** 62))))
+        return out
+
+    calib = draw(64)
+    res, _ = m.serve(calib, budget, inflight)  # includes the one-off autotune
+    res, _ = m.serve(calib, budget, inflight)
+    capacity = len(calib) / max(r["done_s"] for r in res)
+    rate = 0.8 * capacity
+    reqs = draw(n_requests)
+    t = np.cumsum(rng.exponential(1.0 / rate, size=n_requests))
+    for r, a in zip(reqs, t):
+        r["arrival_s"] = float(a)
+    res, _ = m.serve(reqs, budget, inflight)
+    lat = np.array([r["done_s"] - q["arrival_s"] for r, q in zip(res, reqs)])
+    makespan = max(r["done_s"] for r in res) - reqs[0]["arrival_s"]
+    preds = sum(q["n_indiv"] * (q["target_end"] - q["target_begin"]) * 3 for q in reqs)
+    # bytes a request must move: its blocks' input rows in, outputs out
+    req_bytes = 0
+    for q in reqs:
+        lo, hi = m.input_rows(3 * q["target_begin"], 3 * q["target_end"])
+        blocks = (q["n_indiv"] + 1023) // 1024
+        req_bytes += blocks * ((hi - lo) * 8192 + 3 * (q["target_end"] - q["target_begin"]) * 8192)
+    # CPU: the oracle over the first cpu_requests requests (uniform rows of
+    # the same shape; the arithmetic does not depend on the values)
+    rows = np.random.default_rng(seed).integers(0, 2 ** 32, size=(3 * 16184, 2048),
+                                                dtype=np.uint64).astype(np.uint32).view(np.int32)
+    cpu_s, cpu_preds = 0.0, 0
+    for q in reqs[:cpu_requests]:
+        sub = w.model.slice_outputs(3 * q["target_begin"], 3 * q["target_end"])
+        for b in range((q["n_indiv"] + 1023) // 1024):
+            ns = min(1024, q["n_indiv"] - 1024 * b)
+            t1 = time.perf_counter()
+            pyoracle.trlwe_score(sub.term_ptr, sub.term_feat, sub.term_coef, rows, ns, 1, 1024, n_threads=cores())
+            cpu_s += time.perf_counter() - t1
+            cpu_preds += ns * (q["target_end"] - q["target_begin"]) * 3
+    m.free()
+    return {"value": preds / makespan, "requests": n_requests, "requests_per_s": n_requests / makespan,
+            "p50_latency_ms": float(np.percentile(lat, 50) * 1e3), "p99_latency_ms": float(np.percentile(lat, 99) * 1e3),
+            "arrival_rate_per_s": rate, "capacity_per_s": capacity, "max_inflight": inflight,
+            "roofline": hbm_roofline(req_bytes, makespan),
+            "cpu_baseline": {"value": cpu_preds / cpu_s, "unit": UNIT, "cores": cores(), "kind": "port",
+                             "sample": f"{cpu_requests} requests ({cpu_s:.1f} s), oracle restatement"}}
 
 
 def section_decrypt(ctx, model, spec, d_out, seed, steps):
@@ -296,11 +655,7 @@ def section_decrypt(ctx, model, spec, d_out, seed, steps):
     nz = int(key.sum())
     adds = model.n_out * ns * nz
     return {"value": model.n_out * ns / (ms / 1e3), "unit": "decrypted scores/s", "ms_per_step": ms,
-            "rows": model.n_out, "samples": ns, "key_weight": nz,
-            "word_adds_per_s": adds / (ms / 1e3),
-            "kernel": "k_decrypt_binary: 4 rows per CTA, negacyclic extension of each mask in (bank-padded) "
-                      "shared memory, 16 consecutive coefficients per thread, the key in 32-position chunks: a "
-                      "48-word window in registers per chunk, one uniform branch per key bit"}
+            "key_weight": nz, "word_adds_per_s": adds / (ms / 1e3)}
 
 
 def section_encrypt(ctx, spec, seed, steps):
@@ -328,161 +683,8 @@ def section_encrypt(ctx, spec, seed, steps):
     ms = time_on_stream(ctx, run, steps)
     for b in (d_geno, d_src, d_out):
         b.free()
-    return {"value": n_rows / (ms / 1e3), "unit": "TRLWE encryptions/s", "ms_per_step": ms, "rows": n_rows,
-            "samples": ns, "key_weight": int(key.sum()),
-            "kernel": "k_encrypt_binary: 4 rows per CTA, counter-based mask and Box-Muller noise, mask*key as a "
-                      "register-windowed product (16 coefficients per thread), one-hot messages, record headers"}
-
-
-def section_lwe(ctx, name, seed, n_indiv, n_tags, n_targets, neighbours=5, choices=None, passes=2, chunk=2048):
-    """Per-individual LWE form: inputs resident (n_indiv LWE samples of n=1024
-    per feature row), outputs produced range by range into a 2-slot HBM ring
-    (the full output does not fit in HBM)."""
-    from idash2019_2_gb300 import gpu
-    w = gpu.synth_model(seed, n_tags, n_targets, neighbours=neighbours, choices=choices)
-    n_feat = 3 * n_tags
-    stride = gpu.lwe_row_words(n_indiv)
-    L = n_indiv * 1025
-    d_in = ctx.device_alloc(n_feat * stride * 4)
-    gpu.synth_lwe_device(ctx, seed, 1024, n_indiv, n_feat, d_in.ptr, stride)
-    m = gpu.LweModel(ctx, w.model, n_feat, n_indiv)
-    ring = [ctx.device_alloc(chunk * stride * 4) for _ in range(2)]
-    ranges = [(lo, min(lo + chunk, m.n_out)) for lo in range(0, m.n_out, chunk)]
-
-    def one_pass():
-        for c, (lo, hi) in enumerate(ranges):
-            m.score_device(n_indiv, d_in.ptr, stride, lo, hi, ring[c % 2].ptr, stride)
-
-    t0 = time.perf_counter()
-    one_pass()  # first call autotunes the slice width
-    ctx.sync()
-    first_s = time.perf_counter() - t0
-    launches0 = ctx.stats()["kernel_launches"]
-    ms = time_on_stream(ctx, one_pass, passes)
-    launches = (ctx.stats()["kernel_launches"] - launches0) // passes
-    info = m.info()
-    preds = n_indiv * n_targets * 3
-    alg = info["algorithmic_in_rows"] * L * 4 + m.n_out * L * 4 + info["n_terms"] * 8 + m.n_out * 8
-    peak, _ = peaks()
-    macs = float(sum(int(w.model.term_ptr[o + 1] - w.model.term_ptr[o]) - 1 for o in range(0, m.n_out, 97))) * 97
-    out = {"value": preds / (ms / 1e3), "unit": UNIT, "ms_per_step": ms, "workload": name,
-           "individuals": n_indiv, "targets": n_targets, "tags": n_tags,
-           "neighbours": neighbours if not choices else f"uniform from {choices}",
-           "input_bytes": n_feat * stride * 4, "output_bytes_per_step": m.n_out * L * 4,
-           "kernel": KERNEL_NAMES.get(info["kernel"], str(info["kernel"])),
-           "slice_words": info["slice_words"], "launches_per_step": launches,
-           "first_pass_s_including_autotune": first_s,
-           "roofline": {"bound": "hbm", "achieved": alg / (ms / 1e3) / 1e9, "peak": peak, "unit": "GB/s",
-                        "frac": alg / (ms / 1e3) / 1e9 / peak, "algorithmic_bytes_per_step": alg},
-           "int_macs_per_step_est": macs * L, "imad_tops_at_this_rate": macs * L / (ms / 1e3) / 1e12}
-    for b in ring:
-        b.free()
-    d_in.free()
-    m.free()
-    return out
-
-
-def section_intpoly(ctx, seed, passes=5, scale=1):
-    """Integer-polynomial x TRLWE product at full scale: 48,552 input TRLWE
-    (16,184 tags x 3), 242,646 outputs (80,882 targets x 3), 20 neighbours
-    (60 dense int16 weight polynomials per output, |w| <= 8192), one block of
-    1,024 individuals per TRLWE.  Exact (two-prime NTT + CRT).  scale > 1
-    divides the tag and target counts (profiling size)."""
-    import numpy as np
-    from idash2019_2_gb300 import gpu
-    n_tags, n_targets = 16184 // scale, 80882 // scale
-    w = gpu.synth_model(seed, n_tags, n_targets, neighbours=20)
-    csr = w.model
-    const = csr.term_feat == 0xFFFFFFFF
-    counts = np.diff(csr.term_ptr.astype(np.int64)) - np.add.reduceat(const.astype(np.int64),
-                                                                        csr.term_ptr[:-1].astype(np.int64))
-    ptr = np.concatenate([[0], np.cumsum(counts)]).astype(np.uint64)
-    feat = csr.term_feat[~const]
-    bias = np.zeros(csr.n_out, np.int32)
-    owner = np.repeat(np.arange(csr.n_out), np.diff(csr.term_ptr.astype(np.int64)))
-    bias[owner[const]] = csr.term_coef[const]
-    icsr = gpu.CSRModel(ptr, feat, np.zeros(len(feat), np.int32))
-    n_terms, n_rows = len(feat), 3 * n_tags
-    d_poly = ctx.device_alloc(n_terms * 1024 * 2)
-    gpu.synth_int16_device(ctx, seed, n_terms * 1024, 8192, d_poly.ptr)
-    t0 = time.perf_counter()
-    m = gpu.IntpolyModel(ctx, icsr, d_poly.ptr, n_rows, 1024, 1024, bias=bias, poly_on_device=True)
-    build_s = time.perf_counter() - t0
-    d_poly.free()
-    params = gpu.TrlweParams(1024, 1, 1024, 1, 1024, 1 << 18, 42)
-    d_in = ctx.device_alloc(n_rows * 8192)
-    gpu.synth_trlwe_device(ctx, seed, params, n_tags, d_in.ptr, gpu.DENSE_TRLWE)
-    d_out = ctx.device_alloc(csr.n_out * 8192)
-    run = lambda: m.score_device(d_in.ptr, gpu.DENSE_TRLWE, 0, csr.n_out, d_out.ptr, gpu.DENSE_TRLWE)
-    run()
-    ms = time_on_stream(ctx, run, passes)
-    # compulsory traffic of this algorithm per pass: the NTT-domain weights
-    # (2 primes x N words per term), input rows in and their NTT out and back
-    # in, output rows out
-    traffic = n_terms * 2 * 1024 * 4 + n_rows * 8192 + 2 * n_rows * 4 * 1024 * 4 + csr.n_out * 8192
-    peak, _ = peaks()
-    out = {"value": csr.n_out * 1024 / (ms / 1e3), "unit": UNIT, "ms_per_step": ms,
-           "outputs_per_s": csr.n_out / (ms / 1e3), "terms": n_terms, "model_build_s": build_s,
-           "schoolbook_mac_per_s": n_terms * 2 * 1024 * 1024 / (ms / 1e3),
-           "resident_weight_bytes": n_terms * 2 * 1024 * 4,
-           "roofline": {"bound": "hbm", "achieved": traffic / (ms / 1e3) / 1e9, "peak": peak, "unit": "GB/s",
-                        "frac": traffic / (ms / 1e3) / 1e9 / peak, "algorithmic_bytes_per_step": traffic},
-           "workload": f"integer-polynomial x TRLWE: {n_rows:,} input TRLWE, {csr.n_out:,} outputs, 60 dense int16 "
-                       "weight polynomials per output, N=1024, 1,024 individuals per TRLWE (predictions = outputs x "
-                       "1024)"}
-    for b in (d_in, d_out):
-        b.free()
-    m.free()
-    return out
-
-
-def section_serving(ctx, seed, n_requests=10000, budget=150 << 30, inflight=4):
-    """Continuous batching (idash_serve_trlwe) over a Poisson stream: each
-    request has individuals ~ U[1, 2000] and a contiguous target range of
-    length ~ U[1000, 80882]; 10 neighbours; model and index tables resident;
-    150 GB HBM admission budget.  The arrival rate is 0.8 x the measured
-    capacity (64 requests arriving at once)."""
-    import numpy as np
-    from idash2019_2_gb300 import gpu
-    T = 80882
-    w = gpu.synth_model(seed, 16184, T, neighbours=10)
-    m = gpu.TrlweModel(ctx, w.model, 3 * 16184, 1024, 1, 1024)
-    rng = np.random.default_rng(seed)
-
-    def draw(k):
-        out = []
-        for i in range(k):
-            length = int(rng.integers(1000, T + 1))
-            t0 = int(rng.integers(0, T - length + 1))
-            out.append(dict(arrival_s=0.0, n_indiv=int(rng.integers(1, 2001)), target_begin=t0,
-                            target_end=t0 + length, seed=int(rng.integers(1, 2 ** 62))))
-        return out
-
-    calib = draw(64)
-    res, _ = m.serve(calib, budget, inflight)  # includes the one-off autotune
-    res, _ = m.serve(calib, budget, inflight)
-    capacity = len(calib) / max(r["done_s"] for r in res)
-    rate = 0.8 * capacity
-    reqs = draw(n_requests)
-    t = np.cumsum(rng.exponential(1.0 / rate, size=n_requests))
-    for r, a in zip(reqs, t):
-        r["arrival_s"] = float(a)
-    t0 = time.perf_counter()
-    res, _ = m.serve(reqs, budget, inflight)
-    wall = time.perf_counter() - t0
-    lat = np.array([r["done_s"] - q["arrival_s"] for r, q in zip(res, reqs)])
-    makespan = max(r["done_s"] for r in res) - reqs[0]["arrival_s"]
-    preds = sum(q["n_indiv"] * (q["target_end"] - q["target_begin"]) * 3 for q in reqs)
-    m.free()
-    return {"value": preds / makespan, "unit": UNIT, "requests": n_requests, "requests_per_s": n_requests / makespan,
-            "p50_latency_ms": float(np.percentile(lat, 50) * 1e3), "p99_latency_ms": float(np.percentile(lat, 99) * 1e3),
-            "mean_latency_ms": float(lat.mean() * 1e3), "arrival_rate_per_s": rate,
-            "capacity_per_s": capacity, "hbm_budget_bytes": budget, "max_inflight": inflight,
-            "mean_request_device_bytes": float(np.mean([r["device_bytes"] for r in res])),
-            "wall_s": wall,
-            "workload": "Poisson stream of 10,000 requests: individuals ~ U[1,2000] (TRLWE-packed, 1,024 per "
-                        "block), contiguous targets of length ~ U[1000, 80882], 10 neighbours, 150 GB HBM budget; "
-                        "request ciphertexts generated on the device"}
+    return {"value": n_rows / (ms / 1e3), "unit": "TRLWE encryptions/s", "ms_per_step": ms,
+            "key_weight": int(key.sum())}
 
 
 def section_files(seed, small=False):
@@ -548,15 +750,14 @@ def run_sections(ctx, args, sections):
     100 individuals x 2,000 tags x 10,000 targets (a few GB on the device),
     the size the ncu captures under profiles/ use."""
     ni, nt, ng = (100, 2000, 10000) if args.small else (1000, 16184, 80882)
-    scale = f"{ni:,} individuals x {ng:,} targets x 3, {nt:,} tags"
     forms = {}
+    if "config1" in sections:
+        forms["config1"] = section_config1(ctx, args.seed + 5)
     if "lwe_full" in sections:
-        forms["lwe_full"] = section_lwe(ctx, f"per-individual LWE: {scale}, 5 neighbours, n=1024", args.seed,
-                                        ni, nt, ng, neighbours=5)
+        forms["lwe_full"] = section_lwe(ctx, args.seed, ni, nt, ng, neighbours=5, cpu_outputs=512)
     if "batched_uneven" in sections:
-        forms["batched_uneven"] = section_lwe(ctx, f"batched uneven neighbourhoods, per-individual LWE: {scale}, "
-                                                   "neighbours uniform from {5,10,20,30,50}", args.seed + 1,
-                                              ni, nt, ng, choices=[5, 10, 20, 30, 50], passes=1)
+        forms["batched_uneven"] = section_lwe(ctx, args.seed + 1, ni, nt, ng, choices=[5, 10, 20, 30, 50], passes=1,
+                                              cpu_outputs=192)
     if "intpoly" in sections:
         forms["intpoly"] = section_intpoly(ctx, args.seed + 3, scale=64 if args.small else 1)
     if "serving" in sections:
@@ -564,6 +765,23 @@ def run_sections(ctx, args, sections):
     if "files" in sections:
         forms["files"] = section_files(args.seed + 4, small=args.small)
     return forms
+
+
+FORM_WORKLOADS = {
+    "plain": "the headline workload through the plain per-output kernel (k_score_direct)",
+    "kinds": "the headline workload through each batched kernel kind, ms per pass",
+    "config1": "100 individuals x 2,000 targets x 3, 500 tags, 5 neighbours: TRLWE-packed (NUM_REGIONS 10, "
+               "REGION_SIZE 102) and per-individual LWE (n=1024, 0.62 GB in, 2.46 GB out)",
+    "lwe_full": "per-individual LWE at full scale: 1,000 individuals x 80,882 targets x 3, 16,184 tags, 5 neighbours, "
+                "n=1024 (199 GB in, 995 GB out per pass, outputs through a 2-buffer HBM ring)",
+    "batched_uneven": "per-individual LWE at full scale, neighbours uniform from {5,10,20,30,50}",
+    "intpoly": "integer-polynomial x TRLWE: 48,552 input TRLWE, 242,646 outputs, 60 dense int16 weight polynomials "
+               "per output, N=1024, predictions = outputs x 1,024",
+    "serving": "Poisson stream of 10,000 requests: individuals ~ U[1,2000] (TRLWE-packed, 1,024 per block), targets "
+               "~ U[1000, 80882] contiguous, 10 neighbours, 150 GB HBM budget, arrivals at 0.8 x capacity",
+    "encrypt": "party A encryption of the headline's 48,552 input TRLWE",
+    "decrypt": "party A decryption of the headline's 242,646 outputs x 1,000 scores",
+}
 
 
 def run_sections_only(args):
@@ -575,7 +793,7 @@ def run_sections_only(args):
     sections = set(args.sections.split(",")) if args.sections else set()
     forms = run_sections(ctx, args, sections)
     ctx.close()
-    print(json.dumps({"metric": METRIC, "unit": UNIT, "forms": forms}), flush=True)
+    print(json.dumps(sig({"metric": METRIC, "unit": UNIT, "forms": forms})), flush=True)
 
 
 def run_ours(args):
@@ -633,16 +851,15 @@ def run_ours(args):
     ms_step = ms / args.steps
     value = preds_per_step * world / (ms_step / 1e3)
 
-    # algorithmic bytes of one launch: each distinct input TRLWE read once,
-    # each output TRLWE written once, the model's CSR (4 B feature + 4 B
-    # coefficient per term, 4 B bias + 4 B row pointer per output)
-    alg_bytes = info["algorithmic_in_rows"] * 8192 + model.n_out * 8192 + info["n_terms"] * 8 + model.n_out * 8
-    peak, peak_src = peaks()
-    achieved = alg_bytes / (ms_step / 1e3) / 1e9
+    alg_bytes = trlwe_alg_bytes(info, model.n_out)
+    roof = hbm_roofline(alg_bytes, ms_step / 1e3)
     # DRAM bytes of one launch of the kernel kind the autotuner chose, from its
     # ncu capture on this workload (null when that kind has none)
-    traffic = profiled_traffic({0: "trlwe_window_full.txt", 2: "trlwe_pipe_full.txt",
-                                3: "trlwe_ws_full.txt"}.get(info["kernel"], ""))
+    roof["traffic"] = profiled_traffic({0: "trlwe_window_full.txt", 2: "trlwe_pipe_full.txt",
+                                        3: "trlwe_ws_full.txt"}.get(info["kernel"], ""))
+    roof["algorithmic_bytes_per_launch"] = alg_bytes
+    useful = float(np.count_nonzero(w.model.term_feat != CONSTANT)) * 2048
+    roof["imad_frac"] = useful / (ms_step / 1e3) / IMAD_PEAK
 
     # end to end through the host-memory entry point
     e2e_steps = max(3, min(args.steps, 20))
@@ -666,7 +883,7 @@ def run_ours(args):
     base = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         rows = np.frombuffer(h_in.array, dtype=np.int32).reshape(spec["n_rows"], 2048)
-        base = cpu_baseline(w.model, rows, spec)
+        base = cpu_trlwe(w.model.term_ptr, w.model.term_feat, w.model.term_coef, rows, spec, 8.0)
     h_in.free()
     h_out.free()
 
@@ -691,19 +908,14 @@ def run_ours(args):
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": value / PUBLISHED_PREDICTIONS_PER_S if args.workload == "trlwe_full" else None,
-                "dtype": "int32 (Z/2^32)", "data": "synthetic (seeded)",
-                "config": {"workload": spec["desc"], "individuals": spec["n_indiv"], "targets": spec["n_targets"],
-                           "tags": spec["n_tags"], "neighbours": spec["neighbours"], "outputs": model.n_out,
-                           "input_rows": spec["n_rows"], "l2": "inputs 0.40 GB and outputs 1.99 GB exceed the 129 MB L2",
-                           "kernel": KERNEL_NAMES.get(info["kernel"], str(info["kernel"])),
-                           "slice_words": info["slice_words"], "parallelism": f"{world} independent batch(es)"},
-                "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                             "frac": achieved / peak, "traffic": traffic, "peak_source": peak_src,
-                             "algorithmic_bytes_per_launch": alg_bytes},
-                "cpu_baseline": base, "e2e": e2e, "gpu_launches": launches, "clocks": clocks}
+                "dtype": "int32 (Z/2^32)", "data": "synthetic (seeded)", "config": config_of(spec, world),
+                "kernel": {"name": KERNEL_NAMES.get(info["kernel"], str(info["kernel"])),
+                           "slice_words": info["slice_words"]},
+                "roofline": roof, "cpu_baseline": base, "e2e": e2e, "gpu_launches": launches, "clocks": clocks}
         if forms:
             line["forms"] = forms
-        print(json.dumps(line), flush=True)
+            line["form_workloads"] = {k: FORM_WORKLOADS[k] for k in forms if k in FORM_WORKLOADS}
+        print(json.dumps(sig(line)), flush=True)
     ctx.close()
     if world > 1:
         torch.distributed.destroy_process_group()
@@ -718,7 +930,8 @@ def main():
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="trlwe_full")
     ap.add_argument("--seed", type=int, default=0x1DA52019)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--sections", default="plain,kinds,encrypt,decrypt,lwe_full,batched_uneven,intpoly,serving",
+    ap.add_argument("--sections",
+                    default="plain,kinds,config1,encrypt,decrypt,lwe_full,batched_uneven,intpoly,serving",
                     help="extra forms measured after the headline (comma list, '' for none; 'files', the "
                          "cloud step through its files, is opt-in)")
     ap.add_argument("--no-headline", action="store_true",

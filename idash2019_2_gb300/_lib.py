@@ -67,7 +67,8 @@ class Stats(C.Structure):
 class ModelInfo(C.Structure):
     _fields_ = [("n_out", C.c_uint64), ("n_terms", C.c_uint64), ("n_groups", C.c_uint64),
                 ("n_blocks", C.c_uint64), ("n_slots", C.c_uint64), ("slice_words", C.c_uint32),
-                ("max_window_slots", C.c_uint32), ("kernel", C.c_uint32), ("algorithmic_in_rows", C.c_uint64)]
+                ("max_window_slots", C.c_uint32), ("kernel", C.c_uint32), ("algorithmic_in_rows", C.c_uint64),
+                ("dense_k", C.c_uint64)]
 
 
 class SynthSpec(C.Structure):

@@ -797,6 +797,9 @@ idash_status idash_model_get_info(const idash_model *m, idash_model_info *info) 
     info->max_window_slots = m->max_slots;
     info->kernel = uint32_t(m->kind);
     info->algorithmic_in_rows = m->plan.distinct_rows;
+    info->dense_k = 0;
+    if (m->kind == KernelKind::kTc)
+        for (const PlanBlock &b : m->plan.blocks) info->dense_k += b.n_groups;
     return IDASH_OK;
 }
 

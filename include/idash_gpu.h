@@ -262,11 +262,16 @@ idash_status idash_score_intpoly_device(idash_model *model, const void *d_in, co
 idash_status idash_synth_int16_device(idash_ctx *ctx, uint64_t seed, uint64_t n, int32_t max_abs, int16_t *d_out,
                                       void *stream);
 
-/* Model facts: outputs, total terms, planned blocks, slice width chosen. */
+/* Model facts: outputs, total terms, planned blocks, slice width chosen.
+ * kernel: 0 window, 1 direct (plain), 2 pipe, 3 warp-specialised, 4 tensor
+ * cores.  dense_k: tensor-core plans only, the sum over blocks of the padded
+ * K (each block multiplies a 128 x dense_k coefficient matrix per column
+ * slice; 0 for the other kernels). */
 typedef struct {
     uint64_t n_out, n_terms, n_groups, n_blocks, n_slots;
     uint32_t slice_words, max_window_slots, kernel;
     uint64_t algorithmic_in_rows; /* distinct input rows the model reads */
+    uint64_t dense_k;
 } idash_model_info;
 idash_status idash_model_get_info(const idash_model *model, idash_model_info *info);
 /* Re-plans the model for a new kernel / slice choice (after idash_set_option). */
