@@ -575,48 +575,100 @@ def section_intpoly(ctx, seed, passes=5, scale=1, cpu_outputs=24):
     return out
 
 
-def section_serving(ctx, seed, n_requests=10000, budget=150 << 30, inflight=4, cpu_requests=6):
-    """Continuous batching (idash_serve_trlwe) over a Poisson stream: each
-    request has individuals ~ U[1, 2000] and a contiguous target range of
-    length ~ U[1000, 80882]; 10 neighbours; model and index tables resident;
-    150 GB HBM admission budget.  The arrival rate is 0.8 x the measured
-    capacity (64 requests arriving at once)."""
+def section_serving(ctx, seed, n_requests=10000, budget=150 << 30, inflight=16, cpu_requests=6, e2e_requests=200,
+                    lwe_requests=12):
+    """Configuration 5: an online server (idash_server_*) over one resident
+    model with 10 neighbours and a 150 GB HBM admission budget; requests of
+    individuals ~ U[1, 2000] and a contiguous target range of length
+    ~ U[1000, 80882].
+      trlwe      10,000 requests arriving as a Poisson stream at 0.8 x the
+                 measured capacity (TRLWE-packed, 1,024 individuals per block;
+                 ciphertexts generated on the device, outputs digested):
+                 throughput, p50/p99 latency, HBM roofline of the bytes the
+                 requests move, CPU baseline on a sample of requests;
+      e2e        e2e_requests requests with their ciphertexts in page-locked
+                 host memory and their outputs copied back, four in flight
+                 from the client's side (a closed loop);
+      lwe        lwe_requests requests in the per-individual LWE layout
+                 (n = 1024; on average 0.5 TB of outputs each, streamed
+                 through the budget in 2,048-output segments), generated
+                 inputs, digests."""
+    import ctypes as C
+
     import numpy as np
     import pyoracle
     from idash2019_2_gb300 import gpu
     T = 80882
     w = gpu.synth_model(seed, 16184, T, neighbours=10)
-    m = gpu.TrlweModel(ctx, w.model, 3 * 16184, 1024, 1, 1024)
+    ctx.set_option("kernel", 4)  # the server runs the warp-specialised kernel (job tables)
+    try:
+        m = gpu.TrlweModel(ctx, w.model, 3 * 16184, 1024, 1, 1024)
+    finally:
+        ctx.set_option("kernel", 0)
     rng = np.random.default_rng(seed)
 
-    def draw(k):
+    def draw(k, max_indiv=2000):
         out = []
         for i in range(k):
             length = int(rng.integers(1000, T + 1))
             t0 = int(rng.integers(0, T - length + 1))
-            out.append(dict(arrival_s=0.0, n_indiv=int(rng.integers(1, 2001)), target_begin=t0,
+            out.append(dict(arrival_s=0.0, n_indiv=int(rng.integers(1, max_indiv + 1)), target_begin=t0,
                             target_end=t0 + length, seed=int(rng.integers(1, 2 ** 62))))
         return out
 
+    # useful multiply-adds of outputs [0, o): prefix sums of per-output terms
+    live = (w.model.term_feat != CONSTANT).astype(np.int64)
+    term_prefix = np.concatenate([[0], np.cumsum(live)])[w.model.term_ptr.astype(np.int64)]
+
+    def macs(q, row_words, blocks):
+        return float(term_prefix[3 * q["target_end"]] - term_prefix[3 * q["target_begin"]]) * row_words * blocks
+
+    def moved(model, q, row_bytes, blocks):
+        lo, hi = model.input_rows(3 * q["target_begin"], 3 * q["target_end"])
+        return blocks * ((hi - lo) * row_bytes + 3 * (q["target_end"] - q["target_begin"]) * row_bytes)
+
+    def stream(model, qs):
+        """Submits qs at their arrival times (seconds after the server
+        opened) and waits for all; (results, stats, makespan)."""
+        srv = gpu.Server(model, budget, inflight)
+        try:
+            t_open = time.perf_counter()
+            tickets = []
+            for q in qs:
+                while time.perf_counter() - t_open < q["arrival_s"]:
+                    pass
+                tickets.append(srv.submit(q["n_indiv"], q["target_begin"], q["target_end"], seed=q["seed"]))
+            res = [srv.wait(tk) for tk in tickets]
+            st = srv.stats()
+        finally:
+            srv.close()
+        return res, st, max(r["done_s"] for r in res) - qs[0]["arrival_s"]
+
+    def roofline(qs, span, busy_s, row_words, row_bytes, blocks):
+        useful = sum(macs(q, row_words(q), blocks(q)) for q in qs)
+        alg = sum(moved(m_cur, q, row_bytes(q), blocks(q)) for q in qs)
+        roof = compute_roofline(0, useful, 0, alg, span)
+        roof["busy_frac"] = busy_s / span
+        roof["kernel_imad_frac"] = useful / busy_s / IMAD_PEAK
+        roof["kernel_hbm_frac"] = alg / busy_s / 1e9 / peaks()["hbm"]
+        return roof, alg
+
+    trlwe_blocks = lambda q: (q["n_indiv"] + 1023) // 1024
+    m_cur = m
     calib = draw(64)
-    res, _ = m.serve(calib, budget, inflight)  # includes the one-off autotune
-    res, _ = m.serve(calib, budget, inflight)
-    capacity = len(calib) / max(r["done_s"] for r in res)
+    stream(m, calib)
+    cres, cst, cspan = stream(m, calib)
+    capacity = len(calib) / cspan
     rate = 0.8 * capacity
     reqs = draw(n_requests)
     t = np.cumsum(rng.exponential(1.0 / rate, size=n_requests))
     for r, a in zip(reqs, t):
         r["arrival_s"] = float(a)
-    res, _ = m.serve(reqs, budget, inflight)
+    res, st, makespan = stream(m, reqs)
     lat = np.array([r["done_s"] - q["arrival_s"] for r, q in zip(res, reqs)])
-    makespan = max(r["done_s"] for r in res) - reqs[0]["arrival_s"]
     preds = sum(q["n_indiv"] * (q["target_end"] - q["target_begin"]) * 3 for q in reqs)
-    # bytes a request must move: its blocks' input rows in, outputs out
-    req_bytes = 0
-    for q in reqs:
-        lo, hi = m.input_rows(3 * q["target_begin"], 3 * q["target_end"])
-        blocks = (q["n_indiv"] + 1023) // 1024
-        req_bytes += blocks * ((hi - lo) * 8192 + 3 * (q["target_end"] - q["target_begin"]) * 8192)
+    roof, req_bytes = roofline(reqs, makespan, st["busy_s"], lambda q: 2048, lambda q: 8192, trlwe_blocks)
+    croof, _ = roofline(calib, cspan, cst["busy_s"], lambda q: 2048, lambda q: 8192, trlwe_blocks)
     # CPU: the oracle over the first cpu_requests requests (uniform rows of
     # the same shape; the arithmetic does not depend on the values)
     rows = np.random.default_rng(seed).integers(0, 2 ** 32, size=(3 * 16184, 2048),
@@ -630,13 +682,79 @@ def section_serving(ctx, seed, n_requests=10000, budget=150 << 30, inflight=4, c
             pyoracle.trlwe_score(sub.term_ptr, sub.term_feat, sub.term_coef, rows, ns, 1, 1024, n_threads=cores())
             cpu_s += time.perf_counter() - t1
             cpu_preds += ns * (q["target_end"] - q["target_begin"]) * 3
+    out = {"value": preds / makespan, "requests": n_requests, "requests_per_s": n_requests / makespan,
+           "p50_latency_ms": float(np.percentile(lat, 50) * 1e3), "p99_latency_ms": float(np.percentile(lat, 99) * 1e3),
+           "arrival_rate_per_s": rate, "capacity_per_s": capacity, "max_inflight": inflight,
+           "launches": st["launches"], "roofline": roof,
+           "at_capacity": {"requests": len(calib), "value": sum(q["n_indiv"] * (q["target_end"] - q["target_begin"]) * 3
+                                                                for q in calib) / cspan,
+                           "launches": cst["launches"], "roofline": croof},
+           "cpu_baseline": {"value": cpu_preds / cpu_s, "unit": UNIT, "cores": cores(), "kind": "port",
+                            "sample": f"{cpu_requests} requests ({cpu_s:.1f} s), oracle restatement"}}
+
+    # end to end: host payloads through page-locked buffers, four requests
+    # outstanding from the client's side
+    e2e_reqs = draw(e2e_requests)
+    slots = 4
+    max_in = max(2 * (m.input_rows(3 * q["target_begin"], 3 * q["target_end"])[1] -
+                      m.input_rows(3 * q["target_begin"], 3 * q["target_end"])[0]) for q in e2e_reqs) * 8192
+    max_out = max(((q["n_indiv"] + 1023) // 1024) * 3 * (q["target_end"] - q["target_begin"]) for q in e2e_reqs) * 8192
+    bufs = [(ctx.host_alloc(max_in), ctx.host_alloc(max_out)) for _ in range(slots)]
+    for h_in, _ in bufs:
+        h_in.array[:] = np.frombuffer(np.random.default_rng(1).bytes(max_in), np.uint8)
+    srv = gpu.Server(m, budget, inflight)
+    t_open = time.perf_counter()
+    inflight_q, lats, h2d, d2h = [], [], 0, 0
+    try:
+        for i, q in enumerate(e2e_reqs):
+            if len(inflight_q) == slots:
+                tk, ts = inflight_q.pop(0)
+                r = srv.wait(tk)
+                lats.append(r["done_s"] - ts)
+            h_in, h_out = bufs[i % slots]
+            in_shape, out_shape, _ = gpu.serve_input_shape(m, q["n_indiv"], q["target_begin"], q["target_end"])
+            n_in, n_out_b = int(np.prod(in_shape)) * 4, int(np.prod(out_shape)) * 4
+            a_in = np.ctypeslib.as_array((C.c_uint8 * n_in).from_address(h_in.ptr))
+            a_out = np.ctypeslib.as_array((C.c_uint8 * n_out_b).from_address(h_out.ptr))
+            ts = time.perf_counter() - t_open
+            inflight_q.append((srv.submit(q["n_indiv"], q["target_begin"], q["target_end"], h_in=a_in, h_out=a_out), ts))
+            h2d += n_in
+            d2h += n_out_b
+        for tk, ts in inflight_q:
+            r = srv.wait(tk)
+            lats.append(r["done_s"] - ts)
+        wall = time.perf_counter() - t_open
+    finally:
+        srv.close()
+        for a, b in bufs:
+            a.free()
+            b.free()
+    e2e_preds = sum(q["n_indiv"] * (q["target_end"] - q["target_begin"]) * 3 for q in e2e_reqs)
+    out["e2e"] = {"value": e2e_preds / wall, "unit": UNIT, "requests": e2e_requests, "requests_per_s": e2e_requests / wall,
+                  "p50_latency_ms": float(np.percentile(lats, 50) * 1e3),
+                  "p99_latency_ms": float(np.percentile(lats, 99) * 1e3),
+                  "h2d_bytes_per_request": h2d / e2e_requests, "d2h_bytes_per_request": d2h / e2e_requests}
     m.free()
-    return {"value": preds / makespan, "requests": n_requests, "requests_per_s": n_requests / makespan,
-            "p50_latency_ms": float(np.percentile(lat, 50) * 1e3), "p99_latency_ms": float(np.percentile(lat, 99) * 1e3),
-            "arrival_rate_per_s": rate, "capacity_per_s": capacity, "max_inflight": inflight,
-            "roofline": hbm_roofline(req_bytes, makespan),
-            "cpu_baseline": {"value": cpu_preds / cpu_s, "unit": UNIT, "cores": cores(), "kind": "port",
-                             "sample": f"{cpu_requests} requests ({cpu_s:.1f} s), oracle restatement"}}
+
+    # the per-individual LWE layout of configuration 5
+    ctx.set_option("kernel", 4)
+    try:
+        lm = gpu.LweModel(ctx, w.model, 3 * 16184, 2000)
+    finally:
+        ctx.set_option("kernel", 0)
+    m_cur = lm
+    lreqs = draw(lwe_requests)
+    lres, lst, lspan = stream(lm, lreqs)
+    llat = [r["done_s"] - q["arrival_s"] for r, q in zip(lres, lreqs)]
+    lpreds = sum(q["n_indiv"] * (q["target_end"] - q["target_begin"]) * 3 for q in lreqs)
+    lroof, lbytes = roofline(lreqs, lspan, lst["busy_s"], lambda q: q["n_indiv"] * 1025,
+                             lambda q: gpu.lwe_row_words(q["n_indiv"]) * 4, lambda q: 1)
+    out["lwe"] = {"value": lpreds / lspan, "requests": lwe_requests, "launches": lst["launches"],
+                  "p50_latency_ms": float(np.percentile(llat, 50) * 1e3),
+                  "p99_latency_ms": float(np.percentile(llat, 99) * 1e3),
+                  "bytes_moved": lbytes, "roofline": lroof}
+    lm.free()
+    return out
 
 
 def section_decrypt(ctx, model, spec, d_out, seed, steps):
@@ -777,8 +895,10 @@ FORM_WORKLOADS = {
     "batched_uneven": "per-individual LWE at full scale, neighbours uniform from {5,10,20,30,50}",
     "intpoly": "integer-polynomial x TRLWE: 48,552 input TRLWE, 242,646 outputs, 60 dense int16 weight polynomials "
                "per output, N=1024, predictions = outputs x 1,024",
-    "serving": "Poisson stream of 10,000 requests: individuals ~ U[1,2000] (TRLWE-packed, 1,024 per block), targets "
-               "~ U[1000, 80882] contiguous, 10 neighbours, 150 GB HBM budget, arrivals at 0.8 x capacity",
+    "serving": "online server, 10 neighbours, 150 GB HBM budget, individuals ~ U[1,2000], targets ~ U[1000, 80882] "
+               "contiguous: 10,000 Poisson requests at 0.8 x capacity (TRLWE-packed, device-generated inputs, "
+               "digests); e2e: 200 requests with host payloads in page-locked memory; lwe: 12 requests in the "
+               "per-individual LWE layout (n=1024), generated inputs, digests",
     "encrypt": "party A encryption of the headline's 48,552 input TRLWE",
     "decrypt": "party A decryption of the headline's 242,646 outputs x 1,000 scores",
 }

@@ -28,7 +28,7 @@ CONSTANT_FEATURE = 0xFFFFFFFF
 STATUS = {
     0: "IDASH_OK", 1: "IDASH_ERR_INVALID_ARGUMENT", 2: "IDASH_ERR_CUDA", 3: "IDASH_ERR_OUT_OF_MEMORY",
     4: "IDASH_ERR_INDEX", 5: "IDASH_ERR_DEVICE_TIMEOUT", 6: "IDASH_ERR_IO", 7: "IDASH_ERR_FORMAT",
-    8: "IDASH_ERR_UNSUPPORTED", 9: "IDASH_ERR_ADMISSION", 10: "IDASH_ERR_STATE",
+    8: "IDASH_ERR_UNSUPPORTED", 9: "IDASH_ERR_ADMISSION", 10: "IDASH_ERR_STATE", 11: "IDASH_PENDING",
 }
 
 
@@ -93,7 +93,17 @@ class RequestResult(C.Structure):
 
 
 class ServeConfig(C.Structure):
-    _fields_ = [("hbm_budget", C.c_uint64), ("max_inflight", C.c_uint32), ("reserved", C.c_uint32)]
+    _fields_ = [("hbm_budget", C.c_uint64), ("max_inflight", C.c_uint32), ("segment_outputs", C.c_uint32)]
+
+
+class ServeRequest(C.Structure):
+    _fields_ = [("n_indiv", C.c_uint32), ("reserved", C.c_uint32), ("target_begin", C.c_uint64),
+                ("target_end", C.c_uint64), ("h_in", C.c_void_p), ("h_out", C.c_void_p), ("seed", C.c_uint64)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("launches", C.c_uint64), ("requests_done", C.c_uint64), ("busy_s", C.c_double),
+                ("h2d_bytes", C.c_uint64), ("d2h_bytes", C.c_uint64)]
 
 
 class CloudReport(C.Structure):
@@ -148,6 +158,14 @@ PROTOTYPES = {
     "idash_score_trlwe_range": (status_t, [vp, C.c_uint64, C.c_uint64, C.c_uint32, vp, C.POINTER(RowLayout),
                                            C.c_uint64, C.c_uint64, vp, C.POINTER(RowLayout), vp]),
     "idash_model_input_rows": (status_t, [vp, C.c_uint64, C.c_uint64, u64p, u64p]),
+    "idash_server_open": (status_t, [vp, C.POINTER(ServeConfig), C.POINTER(vp)]),
+    "idash_server_submit": (status_t, [vp, C.POINTER(ServeRequest), C.POINTER(C.c_uint64)]),
+    "idash_server_poll": (status_t, [vp, C.c_uint64, C.POINTER(RequestResult)]),
+    "idash_server_wait": (status_t, [vp, C.c_uint64, C.POINTER(RequestResult)]),
+    "idash_server_launches": (C.c_uint64, [vp]),
+    "idash_server_get_stats": (status_t, [vp, C.POINTER(ServerStats)]),
+    "idash_server_close": (status_t, [vp]),
+    "idash_server_last_error": (C.c_char_p, [vp]),
     "idash_serve_trlwe": (status_t, [vp, C.POINTER(ServeConfig), C.POINTER(Request), C.c_uint64,
                                      C.POINTER(RequestResult), C.POINTER(vp)]),
     "idash_digest_host": (C.c_uint64, [u32p, C.c_uint64, C.c_uint64]),

@@ -503,8 +503,42 @@ struct WsStageHeader {
     PlanBlock blk;       // the tile's block
     uint32_t tile;       // tile index, >= n_tiles marks the end of work
     uint32_t next_unit;  // work counter: consumers take (group, part) units from it
-    uint32_t pad[6];
+    uint32_t job;        // multi-job launches: the tile's job
+    uint32_t pad[5];
 };
+
+// Multi-job launches: the job of launch tile `tile` (the last job whose
+// tiles begin at or before it).
+__device__ __forceinline__ uint32_t job_of(const ScoreArgs &a, uint32_t tile) {
+    uint32_t lo = 0, hi = a.n_jobs;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) / 2;
+        if (a.jobs[mid].tile_begin <= tile) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// The launch arguments as one job sees them; `tile` becomes the job's own
+// tile index.
+__device__ __forceinline__ void with_job(ScoreArgs &a, const ScoreJob &j, uint32_t &tile) {
+    tile -= j.tile_begin;
+    a.in = j.in;
+    a.out = j.out;
+    a.digest = j.digest;
+    a.out_lo = j.out_lo;
+    a.out_hi = j.out_hi;
+    a.out_row_base = j.out_row_base;
+    a.digest_base = j.digest_base;
+    a.in_stride = j.stride;
+    a.out_stride = j.stride;
+    a.block_lo = j.block_lo;
+    a.n_blocks = j.n_blocks;
+    a.row_base = j.row_base;
+    a.n_rows = j.n_rows;
+    a.row_words = j.row_words;
+    a.num_samples = j.num_samples;
+}
 static_assert(sizeof(WsStageHeader) == 64, "stage header layout");
 static_assert(2 * kWsMaxStages * 8 + kWsMaxStages * sizeof(WsStageHeader) <= kWsHeaderBytes,
               "barriers and stage headers fit the header area");
@@ -574,25 +608,32 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_score_ws(const ScoreArgs a) {
                 }
                 return;
             }
-            const PlanBlock blk = a.blocks[a.block_lo + tile % a.n_blocks];
-            const uint32_t c0 = (tile / a.n_blocks) * W;
-            const uint32_t valid = min(uint32_t(W), a.row_words - c0);
+            ScoreArgs aj = a;
+            uint32_t lt = tile, job = 0;
+            if (a.n_jobs) {
+                job = job_of(a, tile);
+                with_job(aj, a.jobs[job], lt);
+            }
+            const PlanBlock blk = aj.blocks[aj.block_lo + lt % aj.n_blocks];
+            const uint32_t c0 = (lt / aj.n_blocks) * W;
+            const uint32_t valid = min(uint32_t(W), aj.row_words - c0);
             if (lane == 0) {
                 hdr[s].blk = blk;
                 hdr[s].tile = tile;
                 hdr[s].next_unit = 0;
+                hdr[s].job = job;
             }
             uint32_t *win = win_of(s);
             // rotated slots (NUM_REGIONS > 1): gathered by the producer lanes
             for (uint32_t sl_i = uint32_t(blk.n_slots) - blk.n_rot; sl_i < blk.n_slots; ++sl_i) {
-                const PlanSlot sl = a.slots[blk.slot_begin + sl_i];
-                if (sl.row - a.row_base >= a.n_rows) continue;
+                const PlanSlot sl = aj.slots[blk.slot_begin + sl_i];
+                if (sl.row - aj.row_base >= aj.n_rows) continue;
                 const uint32_t *src =
-                    reinterpret_cast<const uint32_t *>(a.in + uint64_t(sl.row - a.row_base) * a.in_stride);
+                    reinterpret_cast<const uint32_t *>(aj.in + uint64_t(sl.row - aj.row_base) * aj.in_stride);
                 for (uint32_t x = lane; x < valid; x += 32)
-                    win[size_t(sl_i) * W + x] = rotated_word(src, c0 + x, sl.rot, a.N);
+                    win[size_t(sl_i) * W + x] = rotated_word(src, c0 + x, sl.rot, aj.N);
             }
-            issue_tile_loads<W>(a, blk, c0, ((valid + 3u) & ~3u) * 4u, win, terms_of(s), groups_of(s), &full[s],
+            issue_tile_loads<W>(aj, blk, c0, ((valid + 3u) & ~3u) * 4u, win, terms_of(s), groups_of(s), &full[s],
                                 lane);
             pending |= 1u << s;
             // the next tile's index, fetched while this stage's copies fly
@@ -609,25 +650,37 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_score_ws(const ScoreArgs a) {
     }
 
     // --------------------------------------------------------------- consumers
-    uint64_t dig = 0;  // DIG only
+    uint64_t dig = 0;                                 // DIG only
+    unsigned long long *dig_to = a.n_jobs ? nullptr : a.digest;  // where dig goes
+    auto flush_digest = [&]() {
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) dig += __shfl_xor_sync(0xFFFFFFFFu, dig, off);
+        if (lane == 0 && dig && dig_to) atomicAdd(dig_to, (unsigned long long)dig);
+        dig = 0;
+    };
     for (uint32_t it = 0;; ++it) {
         const uint32_t s = it % n_stages, round = it / n_stages;
         if (!mbar_wait_bounded(&full[s], round & 1u, a.err)) return;
         const uint32_t tile = hdr[s].tile;
         if (tile >= a.n_tiles) {
-            if (DIG) {
-#pragma unroll
-                for (int off = 16; off > 0; off >>= 1) dig += __shfl_xor_sync(0xFFFFFFFFu, dig, off);
-                if (lane == 0 && dig) atomicAdd(a.digest, (unsigned long long)dig);
-            }
+            if (DIG) flush_digest();
             return;
         }
+        ScoreArgs aj = a;
+        uint32_t lt = tile;
+        if (a.n_jobs) {
+            with_job(aj, a.jobs[hdr[s].job], lt);
+            if (DIG && aj.digest != dig_to) {  // a new job: the last one's digest is complete here
+                flush_digest();
+                dig_to = aj.digest;
+            }
+        }
         const PlanBlock blk = hdr[s].blk;
-        const uint32_t c0 = (tile / a.n_blocks) * W;
-        const uint32_t valid = min(uint32_t(W), a.row_words - c0);
+        const uint32_t c0 = (lt / aj.n_blocks) * W;
+        const uint32_t valid = min(uint32_t(W), aj.row_words - c0);
         uint32_t bmask[PARTS], zmask[PARTS];
 #pragma unroll
-        for (int p = 0; p < PARTS; ++p) column_masks<Q, TEAM>(a, c0, 32 * p + lane, bmask[p], zmask[p]);
+        for (int p = 0; p < PARTS; ++p) column_masks<Q, TEAM>(aj, c0, 32 * p + lane, bmask[p], zmask[p]);
         const PlanTerm *terms_s = terms_of(s);
         const PlanGroup *groups_s = groups_of(s);
         const uint32_t n_units = blk.n_groups * PARTS;
@@ -651,8 +704,8 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_score_ws(const ScoreArgs a) {
             uint32_t acc[G][4 * Q];
             accumulate_group<W, G, Q, TEAM>(acc, gr, terms_s + gr.term_begin, win_of(s) + 4 * tlane, bias_mask,
                                             zero_mask);
-            write_outputs<G, Q, TEAM>(a, gr, acc, c0, tlane, valid, zero_mask);
-            if (DIG) digest_outputs<W, G, Q, TEAM>(a, gr, acc, c0, tlane, valid, dig);
+            write_outputs<G, Q, TEAM>(aj, gr, acc, c0, tlane, valid, zero_mask);
+            if (DIG && dig_to) digest_outputs<W, G, Q, TEAM>(aj, gr, acc, c0, tlane, valid, dig);
             u = __shfl_sync(0xFFFFFFFFu, u_next, 0);
         }
         __syncwarp();
@@ -854,8 +907,9 @@ int resident_ctas_per_sm(KernelKind kind, uint32_t slice_words, uint32_t group_s
 
 cudaError_t launch_score(KernelKind kind, uint32_t slice_words, uint32_t group_size, const ScoreArgs &a,
                          uint32_t ctas, cudaStream_t stream) {
-    KernelFn fn = a.digest ? pick_digest(kind, slice_words, group_size) : pick_kernel(kind, slice_words, group_size);
-    if (!fn || (a.digest && a.accumulate)) return cudaErrorInvalidValue;
+    const bool dig = a.digest || (a.n_jobs && a.jobs_digest);
+    KernelFn fn = dig ? pick_digest(kind, slice_words, group_size) : pick_kernel(kind, slice_words, group_size);
+    if (!fn || (dig && a.accumulate) || (a.n_jobs && kind != KernelKind::kWs)) return cudaErrorInvalidValue;
     if (a.n_tiles == 0) return cudaSuccess;
     if (kind == KernelKind::kDirect) {
         fn<<<a.n_tiles, kThreads, 0, stream>>>(a);

@@ -11,6 +11,25 @@ namespace idash {
 
 enum : uint32_t { kFormTrlwe = 0, kFormLwe = 1 };
 
+// One job of a multi-job launch (the warp-specialised kernel): a range of
+// plan blocks scored from its own input buffer into its own output buffer,
+// e.g. one block of individuals of one serving request.  Its tiles are
+// [tile_begin, tile_begin + n_blocks * n_slices) of the launch, block-major
+// within a slice as in a single-job launch.
+struct ScoreJob {
+    const uint8_t *in;           // coefficient 0 of the input row holding plan row row_base
+    uint8_t *out;                // coefficient 0 of output row 0 (output out_row_base)
+    unsigned long long *digest;  // the job's digest (null: none)
+    uint64_t out_lo, out_hi;     // outputs written: [out_lo, out_hi)
+    uint64_t out_row_base;
+    uint64_t digest_base;
+    uint64_t stride;             // bytes between rows, inputs and outputs
+    uint32_t block_lo, n_blocks;
+    uint32_t row_base, n_rows;
+    uint32_t row_words, num_samples;
+    uint32_t tile_begin, n_slices;
+};
+
 struct ScoreArgs {
     const PlanBlock *blocks;
     const PlanSlot *slots;
@@ -53,6 +72,12 @@ struct ScoreArgs {
     uint32_t unit_slices, units_per_block, n_units;
     uint32_t tc_a_max_bytes;      // shared-memory room for one block's digits
     uint32_t tc_use_map;          // set by the launch: consecutive-row chunks come by 2D tensor copy
+    // Multi-job launches (KernelKind::kWs only): n_jobs > 0 replaces the
+    // per-launch input, output, row window, columns, bias rows and digest by
+    // the job of each tile; jobs sorted by tile_begin, n_tiles their total.
+    // jobs_digest: some job takes a digest (the fused-digest instance runs).
+    const ScoreJob *jobs;
+    uint32_t n_jobs, jobs_digest;
 };
 
 // kWindow: persistent, 256 threads, one shared-memory buffer, 1-2 CTAs/SM.

@@ -333,6 +333,11 @@ class LweModel:
         except Exception:
             pass
 
+    def input_rows(self, out_begin: int, out_end: int) -> tuple[int, int]:
+        lo, hi = C.c_uint64(), C.c_uint64()
+        self.ctx.check(self.ctx.lib.idash_model_input_rows(self.h, out_begin, out_end, C.byref(lo), C.byref(hi)))
+        return lo.value, hi.value
+
     def info(self) -> dict:
         i = _lib.ModelInfo()
         self.ctx.check(self.ctx.lib.idash_model_get_info(self.h, C.byref(i)))
@@ -385,6 +390,79 @@ class IntpolyModel:
         self.ctx.check(self.ctx.lib.idash_score_intpoly_device(
             self.h, C.c_void_p(d_in), C.byref(in_layout), out_begin, out_end, C.c_void_p(d_out), C.byref(out_layout),
             C.c_void_p(stream) if stream else None))
+
+
+class Server:
+    """An online serving engine over one resident model (idash_server_*):
+    submit requests at any time, poll or wait for their results."""
+
+    def __init__(self, model, hbm_budget: int, max_inflight: int, segment_outputs: int = 0):
+        self.ctx, self.model = model.ctx, model
+        lib = self.ctx.lib
+        cfg = _lib.ServeConfig(hbm_budget, max_inflight, segment_outputs)
+        h = C.c_void_p()
+        self.ctx.check(lib.idash_server_open(model.h, C.byref(cfg), C.byref(h)))
+        self.h = h
+        self._keep = {}
+
+    def submit(self, n_indiv: int, target_begin: int, target_end: int, h_in=None, h_out=None, seed: int = 0) -> int:
+        """h_in / h_out: numpy arrays (kept alive until the request is waited
+        for) or None (inputs generated from seed / digest only)."""
+        r = _lib.ServeRequest(n_indiv, 0, target_begin, target_end,
+                              None if h_in is None else h_in.ctypes.data, None if h_out is None else h_out.ctypes.data,
+                              seed)
+        t = C.c_uint64()
+        code = self.ctx.lib.idash_server_submit(self.h, C.byref(r), C.byref(t))
+        if code != 0:
+            raise IdashError(code, (self.ctx.lib.idash_server_last_error(self.h) or b"").decode())
+        self._keep[t.value] = (h_in, h_out)
+        return t.value
+
+    def poll(self, ticket: int):
+        res = _lib.RequestResult()
+        code = self.ctx.lib.idash_server_poll(self.h, ticket, C.byref(res))
+        if code == 11:
+            return None
+        if code != 0:
+            raise IdashError(code, (self.ctx.lib.idash_server_last_error(self.h) or b"").decode())
+        return {k: getattr(res, k) for k, _ in res._fields_}
+
+    def wait(self, ticket: int) -> dict:
+        res = _lib.RequestResult()
+        code = self.ctx.lib.idash_server_wait(self.h, ticket, C.byref(res))
+        if code != 0:
+            raise IdashError(code, (self.ctx.lib.idash_server_last_error(self.h) or b"").decode())
+        self._keep.pop(ticket, None)
+        return {k: getattr(res, k) for k, _ in res._fields_}
+
+    def launches(self) -> int:
+        return self.ctx.lib.idash_server_launches(self.h)
+
+    def stats(self) -> dict:
+        """launches, requests_done, busy_s (device time of the scoring
+        launches), h2d_bytes and d2h_bytes since the server opened."""
+        st = _lib.ServerStats()
+        self.ctx.check(self.ctx.lib.idash_server_get_stats(self.h, C.byref(st)))
+        return {k: getattr(st, k) for k, _ in st._fields_}
+
+    def close(self):
+        if self.h:
+            h, self.h = self.h, None
+            self.ctx.check(self.ctx.lib.idash_server_close(h))
+            self._keep.clear()
+
+
+def serve_input_shape(model, n_indiv: int, target_begin: int, target_end: int):
+    """(input rows shape, output rows shape, first input row) of a served
+    request: TRLWE (blocks, rows, 2N) int32, LWE (rows, stride) int32."""
+    lo, hi = model.input_rows(3 * target_begin, 3 * target_end)
+    n_out = 3 * (target_end - target_begin)
+    if isinstance(model, LweModel):
+        stride = lwe_row_words(n_indiv, model.n)
+        return (hi - lo, stride), (n_out, stride), lo
+    rs = model.params.region_size
+    blocks = (n_indiv + rs - 1) // rs
+    return (blocks, hi - lo, 2 * model.N), (blocks, n_out, 2 * model.N), lo
 
 
 def synth_int16_device(ctx: Context, seed: int, n: int, max_abs: int, d_out: int):

@@ -43,7 +43,8 @@ typedef enum {
     IDASH_ERR_FORMAT = 7,           /* malformed params.bin / model / ciphertext file */
     IDASH_ERR_UNSUPPORTED = 8,      /* parameter outside what the kernels implement (k != 1 ...) */
     IDASH_ERR_ADMISSION = 9,        /* serving: request can never fit the HBM budget */
-    IDASH_ERR_STATE = 10            /* call out of order (e.g. score before a model is loaded) */
+    IDASH_ERR_STATE = 10,           /* call out of order (e.g. score before a model is loaded) */
+    IDASH_PENDING = 11              /* serving: the request is still in flight (idash_server_poll) */
 } idash_status;
 
 typedef struct idash_ctx idash_ctx;     /* one device, one stream, scratch, error word */
@@ -172,15 +173,90 @@ idash_status idash_model_input_rows(const idash_model *model, uint64_t out_begin
 
 /* ------------------------------------------- serving (continuous batching)
  * No counterpart in the reference (its cloud binary scores one batch per
- * process).  Serves a stream of imputation requests against one resident
- * TRLWE model planned with NUM_REGIONS = 1: a request is n_indiv individuals
- * (packed REGION_SIZE per TRLWE block) and the targets
- * [target_begin, target_end) (outputs 3*target_begin .. 3*target_end).
- * Requests are admitted in arrival order while a stream slot is free and
- * their device memory fits hbm_budget; admitted requests run concurrently.
- * Each request's ciphertexts are generated on the device (block b of a
- * request: idash_synth_uniform_device with seed = seed * 0x9E3779B97F4A7C15 + b,
- * rows [row_begin, row_end) of idash_model_input_rows), scored, and digested. */
+ * process, eval/cloud.cpp:3-28).  A server keeps one model resident (TRLWE
+ * planned with NUM_REGIONS = 1, or LWE; planned for the warp-specialised
+ * kernel, "kernel" option 4 or autotuned to it) and serves imputation
+ * requests submitted at any time, from any thread, while others run.
+ *
+ * A request is n_indiv individuals and the contiguous targets
+ * [target_begin, target_end): outputs 3*target_begin .. 3*target_end, which
+ * read the input rows [row_begin, row_end) of idash_model_input_rows.
+ *   TRLWE: individuals packed REGION_SIZE per block, ceil(n_indiv /
+ *     REGION_SIZE) blocks; input: blocks x (row_end - row_begin) rows, output:
+ *     blocks x (3 * targets) rows, dense 2N int32 rows (block-major).
+ *   LWE: input: (row_end - row_begin) rows, output: 3 * targets rows, each of
+ *     n_indiv samples of n+1 int32 at a stride of n_indiv*(n+1) rounded up to
+ *     a multiple of 4 words; n_indiv at most the model's.
+ * h_in NULL: the inputs are generated on the device from `seed` (TRLWE
+ * block b: idash_synth_uniform_device with seed * 0x9E3779B97F4A7C15 + b; LWE
+ * the same with b = 0, row_words n_indiv*(n+1)); h_out NULL: only the digest
+ * is kept.  Host buffers should be page-locked (idash_host_alloc) for
+ * full-speed copies, and stay untouched until the request completes.
+ *
+ * The scheduler admits requests in submission order while fewer than
+ * max_inflight are admitted and the HBM budget holds their inputs and one
+ * output segment (segment_outputs outputs; 0 = all of a TRLWE request, 2,048
+ * for LWE).  Every launch scores the staged segments of all admitted
+ * requests together (onto an idle device, about half of them, so that the
+ * next launch is queued behind it): one persistent kernel over a job table.  Inputs are
+ * copied in and outputs out on their own streams, overlapped with the
+ * launches.  A request's outputs and digest do not depend on what else runs
+ * beside it.  While a server runs on a model, use the model only through it. */
+typedef struct idash_server idash_server;
+typedef struct {
+    uint64_t hbm_budget;      /* device bytes the admitted requests may hold together */
+    uint32_t max_inflight;    /* requests admitted at once, 1 .. 4096 */
+    uint32_t segment_outputs; /* outputs per segment (0: the form's default) */
+} idash_serve_config;
+typedef struct {
+    uint32_t n_indiv;                  /* individuals in the request */
+    uint32_t reserved;
+    uint64_t target_begin, target_end; /* contiguous target SNPs */
+    const void *h_in;                  /* host input rows, or NULL: generated from seed */
+    void *h_out;                       /* host output rows, or NULL: digest only */
+    uint64_t seed;
+} idash_serve_request;
+typedef struct {
+    double admit_s;        /* admission, seconds after idash_server_open (host clock) */
+    double done_s;         /* completion: outputs in h_out (or scored), seconds after open (CUDA events) */
+    uint64_t device_bytes; /* HBM the request held at admission (inputs + one output segment) */
+    uint64_t digest;       /* sum mod 2^64 over its output words of a 32-bit hash of (index, word),
+                              index = word position in the output layout above; idash_digest_host
+                              restates it */
+} idash_request_result;
+
+idash_status idash_server_open(idash_model *model, const idash_serve_config *config, idash_server **server);
+/* Queues a request; *ticket names it.  Fails with IDASH_ERR_ADMISSION when
+ * the request could never fit the budget, IDASH_ERR_INVALID_ARGUMENT when it
+ * is empty or out of range. */
+idash_status idash_server_submit(idash_server *server, const idash_serve_request *request, uint64_t *ticket);
+/* IDASH_OK and *result when the request is complete, IDASH_PENDING while it
+ * is in flight, or the request's error. */
+idash_status idash_server_poll(idash_server *server, uint64_t ticket, idash_request_result *result);
+/* Blocks until the request completes (or fails). */
+idash_status idash_server_wait(idash_server *server, uint64_t ticket, idash_request_result *result);
+/* Kernel launches so far (each scores the segments staged at that time). */
+uint64_t idash_server_launches(const idash_server *server);
+typedef struct {
+    uint64_t launches;       /* scoring launches issued */
+    uint64_t requests_done;  /* requests completed */
+    double busy_s;           /* device time of the completed scoring launches, summed (CUDA events) */
+    uint64_t h2d_bytes;      /* request input bytes copied in from host memory */
+    uint64_t d2h_bytes;      /* request output bytes copied out to host memory */
+} idash_server_stats;
+/* Counters since idash_server_open; busy_s / elapsed time is the share of the
+ * time the device spent scoring. */
+idash_status idash_server_get_stats(idash_server *server, idash_server_stats *stats);
+/* Finishes every submitted request, then frees the server. */
+idash_status idash_server_close(idash_server *server);
+/* Why the server failed, else why the last refused submit was refused ("" if neither). */
+const char *idash_server_last_error(const idash_server *server);
+
+/* The whole stream in one call, on a server opened for it: request i is
+ * submitted at arrival_s seconds after the start (synthetic inputs from
+ * seed, outputs to host_out[i] when non-NULL) and results[i] filled.  A
+ * request larger than the budget fails with IDASH_ERR_ADMISSION before
+ * anything runs.  TRLWE models only. */
 typedef struct {
     double arrival_s;                  /* seconds after the run starts */
     uint32_t n_indiv;                  /* individuals in the request */
@@ -188,22 +264,6 @@ typedef struct {
     uint64_t target_begin, target_end; /* contiguous target SNPs */
     uint64_t seed;                     /* the request's synthetic ciphertexts */
 } idash_request;
-typedef struct {
-    double admit_s;        /* admission, seconds after the start (host clock) */
-    double done_s;         /* device completion, seconds after the start (CUDA events) */
-    uint64_t device_bytes; /* HBM the request held while in flight */
-    uint64_t digest;       /* sum mod 2^64 over its output words of a 32-bit hash of (index, word);
-                              idash_digest_host restates it */
-} idash_request_result;
-typedef struct {
-    uint64_t hbm_budget;   /* device bytes the in-flight requests may hold together */
-    uint32_t max_inflight; /* concurrent requests (one stream each), 1..64 */
-    uint32_t reserved;
-} idash_serve_config;
-/* Runs the whole stream (requests sorted by arrival_s) and fills results[i].
- * host_out (optional) receives request i's output rows (blocks x outputs x
- * 2N int32) in host_out[i] when non-NULL.  A request larger than the budget
- * fails with IDASH_ERR_ADMISSION before anything runs. */
 idash_status idash_serve_trlwe(idash_model *model, const idash_serve_config *config, const idash_request *requests,
                                uint64_t n_requests, idash_request_result *results, void *const *host_out);
 /* Host restatement of the serving digest, for checking results. */

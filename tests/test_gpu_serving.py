@@ -138,3 +138,125 @@ def test_requests_beyond_the_budget_are_refused(served):
     with pytest.raises(gpu.IdashError) as e:
         m.serve([big], hbm_budget=64 << 20, max_inflight=2)
     assert e.value.name == "IDASH_ERR_ADMISSION"
+
+
+# ------------------------------------------------------------ online server
+def _rows_for(rng, shape):
+    return rng.integers(0, 2 ** 32, size=shape, dtype=np.uint64).astype(np.uint32).view(np.int32)
+
+
+def test_online_server_host_payloads_match_the_oracle(served, oracle):
+    """Requests submitted one after another while earlier ones run, with
+    their ciphertexts in host memory and their outputs copied back: every
+    output word equals the oracle's, and each request's outputs and digest
+    are the same when it is served alone."""
+    import ctypes as C
+    ctx, w, m, _, _, _ = served
+    rng = np.random.default_rng(11)
+    srv = gpu.Server(m, hbm_budget=1 << 30, max_inflight=6)
+    reqs, tickets = [], []
+    try:
+        for i in range(12):
+            length = int(rng.integers(10, 300))
+            t0 = int(rng.integers(0, 1000 - length))
+            n_indiv = int(rng.integers(1, 2200))
+            in_shape, out_shape, lo = gpu.serve_input_shape(m, n_indiv, t0, t0 + length)
+            h_in = _rows_for(rng, in_shape)
+            h_out = np.zeros(out_shape, np.int32)
+            tickets.append(srv.submit(n_indiv, t0, t0 + length, h_in=h_in, h_out=h_out))
+            reqs.append((n_indiv, t0, t0 + length, h_in, h_out, lo))
+            if i % 4 == 3:
+                srv.wait(tickets[-2])  # later requests arrive while others are in flight
+        res = [srv.wait(t) for t in tickets]
+        launches = srv.launches()
+        st = srv.stats()
+    finally:
+        srv.close()
+    assert launches <= len(reqs)
+    # the counters: every payload byte crossed once each way, device time was spent
+    assert st["launches"] == launches and st["requests_done"] == len(reqs)
+    assert st["h2d_bytes"] == sum(q[3].nbytes for q in reqs)
+    assert st["d2h_bytes"] == sum(q[4].nbytes for q in reqs)
+    assert 0 < st["busy_s"] < max(r["done_s"] for r in res)
+    for (n_indiv, t0, t1, h_in, h_out, lo), r in zip(reqs, res):
+        sub = w.model.slice_outputs(3 * t0, 3 * t1)
+        for b in range(h_in.shape[0]):
+            rows = np.zeros((900, 2048), np.int32)
+            rows[lo:lo + h_in.shape[1]] = h_in[b]
+            ns = min(1024, n_indiv - 1024 * b)
+            want, _ = oracle.trlwe_score(sub.term_ptr, sub.term_feat, sub.term_coef, rows, ns, 1, 1024)
+            np.testing.assert_array_equal(h_out[b], want)
+        words = np.ascontiguousarray(h_out).view(np.uint32).ravel()
+        assert r["digest"] == ctx.lib.idash_digest_host(words.ctypes.data_as(C.POINTER(C.c_uint32)), words.size, 0)
+    # alone: one request at a time
+    alone = gpu.Server(m, hbm_budget=1 << 30, max_inflight=1)
+    try:
+        for (n_indiv, t0, t1, h_in, h_out, lo), r in list(zip(reqs, res))[:4]:
+            out1 = np.zeros_like(h_out)
+            r1 = alone.wait(alone.submit(n_indiv, t0, t1, h_in=h_in, h_out=out1))
+            np.testing.assert_array_equal(out1, h_out)
+            assert r1["digest"] == r["digest"]
+    finally:
+        alone.close()
+
+
+def test_online_server_lwe_form_in_segments(oracle):
+    """The per-individual LWE form served: requests of different individual
+    counts (different row strides) share launches, outputs come back in
+    segments of 37 outputs; every word equals the oracle's."""
+    import ctypes as C
+    ctx = gpu.Context(0)
+    try:
+        n, n_tags = 1024, 200
+        w = gpu.synth_model(seed=21, n_tags=n_tags, n_targets=300, neighbours=10)
+        m = gpu.LweModel(ctx, w.model, 3 * n_tags, 40, n)
+        rng = np.random.default_rng(3)
+        srv = gpu.Server(m, hbm_budget=1 << 30, max_inflight=4, segment_outputs=37)
+        reqs, tickets = [], []
+        try:
+            for i in range(7):
+                length = int(rng.integers(5, 120))
+                t0 = int(rng.integers(0, 300 - length))
+                n_indiv = int(rng.integers(1, 41))
+                in_shape, out_shape, lo = gpu.serve_input_shape(m, n_indiv, t0, t0 + length)
+                h_in = _rows_for(rng, in_shape)
+                h_out = np.zeros(out_shape, np.int32)
+                tickets.append(srv.submit(n_indiv, t0, t0 + length, h_in=h_in, h_out=h_out))
+                reqs.append((n_indiv, t0, t0 + length, h_in, h_out, lo))
+            res = [srv.wait(t) for t in tickets]
+        finally:
+            srv.close()
+        for (n_indiv, t0, t1, h_in, h_out, lo), r in zip(reqs, res):
+            L = n_indiv * (n + 1)
+            sub = w.model.slice_outputs(3 * t0, 3 * t1)
+            rows = np.zeros((3 * n_tags, h_in.shape[1]), np.int32)
+            rows[lo:lo + h_in.shape[0]] = h_in
+            want = oracle.lwe_score(sub.term_ptr, sub.term_feat, sub.term_coef, rows, n_indiv, 0, sub.n_out, n=n)
+            np.testing.assert_array_equal(h_out[:, :L], want)
+            # the digest covers the valid words at their positions in the output layout
+            exp = 0
+            for row in range(h_out.shape[0]):
+                words = np.ascontiguousarray(h_out[row, :L]).view(np.uint32)
+                exp += ctx.lib.idash_digest_host(words.ctypes.data_as(C.POINTER(C.c_uint32)), L, row * h_out.shape[1])
+            assert r["digest"] == exp % (1 << 64)
+        m.free()
+    finally:
+        ctx.close()
+
+
+def test_online_server_refuses_bad_requests(served):
+    ctx, w, m, _, _, _ = served
+    srv = gpu.Server(m, hbm_budget=64 << 20, max_inflight=2)
+    try:
+        with pytest.raises(gpu.IdashError) as e:
+            srv.submit(3000, 0, 1000)  # more than the budget
+        assert e.value.name == "IDASH_ERR_ADMISSION"
+        with pytest.raises(gpu.IdashError) as e:
+            srv.submit(10, 990, 1001)  # targets out of range
+        assert e.value.name == "IDASH_ERR_INVALID_ARGUMENT"
+        t = srv.submit(5, 0, 10, seed=9)
+        r = srv.wait(t)
+        assert r["done_s"] >= r["admit_s"] >= 0
+        assert srv.poll(t)["digest"] == r["digest"]
+    finally:
+        srv.close()
