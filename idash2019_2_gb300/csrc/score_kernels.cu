@@ -33,28 +33,39 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
 }
 
 // Epilogue masks over the thread's 4Q columns (bit 4k+e: quad k, element e):
-// which columns receive the bias, which are zeroed.
+// which columns receive the bias, which are zeroed.  Worked out per quad: a
+// quad's four columns are consecutive and start at a multiple of 4, and N is
+// a multiple of 256, so a TRLWE quad lies wholly in the mask part (columns
+// < N) or wholly in the body part.
 template <int Q, int TEAM>
 __device__ __forceinline__ void column_masks(const ScoreArgs &a, uint32_t c0, uint32_t lane, uint32_t &bias_mask,
                                              uint32_t &zero_mask) {
     bias_mask = 0;
     zero_mask = 0;
 #pragma unroll
-    for (int k = 0; k < Q; ++k)
+    for (int k = 0; k < Q; ++k) {
+        const uint32_t c = c0 + 4 * lane + 4 * k * TEAM;  // the quad's first column
+        uint32_t b = 0, z = 0;
+        if (a.form == kFormTrlwe) {
+            if (c >= a.N) {
+                const uint32_t j = c - a.N;  // body coefficients j .. j+3
+                // coefficients below NUM_SAMPLES take the bias
+                if (j < a.num_samples) b = 0xFu >> (4u - min(a.num_samples - j, 4u));
+                // coefficients from REGION_SIZE on are zeroed
+                if (j + 4u > a.region_size) z = (0xFu << (a.region_size > j ? a.region_size - j : 0u)) & 0xFu;
+            }
+        } else {
+            // LWE: column c+e is a sample's body word when (c+e) % (n+1) == n
+            uint32_t r = c % a.lwe_n1;
 #pragma unroll
-        for (int e = 0; e < 4; ++e) {
-            const uint32_t c = c0 + 4 * lane + 4 * k * TEAM + e;
-            const uint32_t bit = 1u << (4 * k + e);
-            if (a.form == kFormTrlwe) {
-                if (c >= a.N) {
-                    const uint32_t j = c - a.N;
-                    if (j < a.num_samples) bias_mask |= bit;
-                    if (j >= a.region_size) zero_mask |= bit;
-                }
-            } else if (c % a.lwe_n1 == a.lwe_n1 - 1) {
-                bias_mask |= bit;
+            for (int e = 0; e < 4; ++e) {
+                if (r == a.lwe_n1 - 1) b |= 1u << e;
+                r = r + 1 == a.lwe_n1 ? 0u : r + 1;
             }
         }
+        bias_mask |= b << (4 * k);
+        zero_mask |= z << (4 * k);
+    }
 }
 
 __device__ __forceinline__ void store_quad(uint8_t *row, uint32_t q, uint32_t valid, uint4 v) {
@@ -95,17 +106,23 @@ template <int G, int Q, int TEAM>
 __device__ __forceinline__ void write_outputs(const ScoreArgs &a, const PlanGroup &gr, uint32_t (&acc)[G][4 * Q],
                                               uint32_t c0, uint32_t lane, uint32_t valid, uint32_t zero_mask) {
     constexpr uint32_t W = 4 * Q * TEAM;
+    // Output ordinals, output rows and the row stride are below 2^32 (the
+    // launch checks the stride): 32-bit compares and one wide multiply-add
+    // per row address.
+    const uint32_t lo = uint32_t(min(a.out_lo, uint64_t(kNoOutput)));
+    const uint32_t hi = uint32_t(min(a.out_hi, uint64_t(kNoOutput)));
+    uint8_t *const out_c0 = a.out + uint64_t(c0) * 4;
 #pragma unroll
     for (int m = 0; m < G; ++m) {
         const uint32_t o = gr.out[m];
-        if (o == kNoOutput || o < a.out_lo || o >= a.out_hi) continue;
+        if (o - lo >= hi - lo) continue;  // outside [out_lo, out_hi), kNoOutput included
         if (zero_mask) {
 #pragma unroll
             for (int e = 0; e < 4 * Q; ++e)
                 if (zero_mask & (1u << e)) acc[m][e] = 0;
         }
-        const uint64_t r = a.out_row_map ? uint64_t(a.out_row_map[o]) : uint64_t(o) - a.out_row_base;
-        uint8_t *row = a.out + r * a.out_stride + uint64_t(c0) * 4;
+        const uint32_t r = a.out_row_map ? a.out_row_map[o] : o - uint32_t(a.out_row_base);
+        uint8_t *row = out_c0 + uint64_t(r) * uint32_t(a.out_stride);
         if (a.accumulate) {
             // a later part of a split group: add what the earlier launches
             // wrote (zeroed columns stay zero: both terms are zero there)
@@ -610,7 +627,7 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_score_ws(const ScoreArgs a) {
             }
             ScoreArgs aj = a;
             uint32_t lt = tile, job = 0;
-            if (a.n_jobs) {
+            if (DIG && a.n_jobs) {
                 job = job_of(a, tile);
                 with_job(aj, a.jobs[job], lt);
             }
@@ -668,7 +685,7 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_score_ws(const ScoreArgs a) {
         }
         ScoreArgs aj = a;
         uint32_t lt = tile;
-        if (a.n_jobs) {
+        if (DIG && a.n_jobs) {
             with_job(aj, a.jobs[hdr[s].job], lt);
             if (DIG && aj.digest != dig_to) {  // a new job: the last one's digest is complete here
                 flush_digest();
@@ -907,9 +924,12 @@ int resident_ctas_per_sm(KernelKind kind, uint32_t slice_words, uint32_t group_s
 
 cudaError_t launch_score(KernelKind kind, uint32_t slice_words, uint32_t group_size, const ScoreArgs &a,
                          uint32_t ctas, cudaStream_t stream) {
-    const bool dig = a.digest || (a.n_jobs && a.jobs_digest);
+    // job tables run on the fused-digest instances (a job without a digest
+    // pointer takes none)
+    const bool dig = a.digest || a.n_jobs;
     KernelFn fn = dig ? pick_digest(kind, slice_words, group_size) : pick_kernel(kind, slice_words, group_size);
     if (!fn || (dig && a.accumulate) || (a.n_jobs && kind != KernelKind::kWs)) return cudaErrorInvalidValue;
+    if (a.out_stride > 0xFFFFFFFFull) return cudaErrorInvalidValue;  // write_outputs' 32-bit row addressing
     if (a.n_tiles == 0) return cudaSuccess;
     if (kind == KernelKind::kDirect) {
         fn<<<a.n_tiles, kThreads, 0, stream>>>(a);

@@ -75,9 +75,10 @@ struct ScoreArgs {
     // Multi-job launches (KernelKind::kWs only): n_jobs > 0 replaces the
     // per-launch input, output, row window, columns, bias rows and digest by
     // the job of each tile; jobs sorted by tile_begin, n_tiles their total.
-    // jobs_digest: some job takes a digest (the fused-digest instance runs).
+    // They run on the fused-digest instance (a job whose digest pointer is
+    // null takes none), so the plain instance carries no per-job state.
     const ScoreJob *jobs;
-    uint32_t n_jobs, jobs_digest;
+    uint32_t n_jobs;
 };
 
 // kWindow: persistent, 256 threads, one shared-memory buffer, 1-2 CTAs/SM.

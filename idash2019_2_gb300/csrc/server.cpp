@@ -408,7 +408,6 @@ bool idash_server::launch() {
     a.err = ctx->d_err;
     a.jobs = d_jobs[k];
     a.n_jobs = uint32_t(jobs.size());
-    a.jobs_digest = 1;
     if (!check(cudaEventRecord(launch_start[k], compute), "event")) return false;
     if (!check(launch_score(KernelKind::kWs, W, m->group_size, a, m->ctas, compute), "scoring launch")) return false;
     if (!check(cudaEventRecord(launch_done[k], compute), "event")) return false;
