@@ -548,6 +548,23 @@ def section_intpoly(ctx, seed, passes=5, scale=1, cpu_outputs=24):
     run = lambda: m.score_device(d_in.ptr, gpu.DENSE_TRLWE, 0, csr.n_out, d_out.ptr, gpu.DENSE_TRLWE)
     run()
     ms = time_on_stream(ctx, run, passes)
+    # The stored-form trade: resident transformed weights (2 primes x 1,024
+    # words = 8 KiB a term, read every pass) against int16 weights (2 KiB a
+    # term) transformed on every pass.  The transform's own time bounds what
+    # any pass that starts from int16 weights costs above the scoring.
+    d_w16 = ctx.device_alloc(n_terms * 1024 * 2)
+    gpu.synth_int16_device(ctx, seed, n_terms * 1024, 8192, d_w16.ptr)  # the same weights again
+    transform = lambda: m.set_weights(d_w16.ptr)
+    transform()
+    transform_ms = time_on_stream(ctx, transform, passes)
+    alt_ms = time_on_stream(ctx, lambda: (transform(), run()), passes)
+    d_w16.free()
+    weights = {"resident_transform": {"bytes_per_term": 8192, "ms_per_step": ms},
+               "int16_transformed_each_pass": {"bytes_per_term": 2048, "ms_per_step": alt_ms,
+                                               "transform_ms": transform_ms,
+                                               "transform_hbm_frac": hbm_roofline(n_terms * (2048 + 8192),
+                                                                                  transform_ms / 1e3)["frac"]},
+               "kept": "resident_transform" if ms <= alt_ms else "int16_transformed_each_pass"}
     rows = d_in.download(dtype=np.int32).reshape(n_rows, 2048)
     t1 = time.perf_counter()
     pyoracle.intpoly_score(ptr[:cpu_outputs + 1], feat[:int(ptr[cpu_outputs])], polys, bias[:cpu_outputs], rows,
@@ -563,6 +580,7 @@ def section_intpoly(ctx, seed, passes=5, scale=1, cpu_outputs=24):
     out = {"value": csr.n_out * 1024 / (ms / 1e3), "ms_per_step": ms, "outputs_per_s": csr.n_out / (ms / 1e3),
            "terms": n_terms, "model_build_s": build_s,
            "schoolbook_mac_per_s": n_terms * 2 * 1024 * 1024 / (ms / 1e3),
+           "weights": weights,
            "roofline": hbm_roofline(alg, ms / 1e3),
            "representation": {"bytes_per_step": traffic, "over_config_bytes": traffic / alg,
                               "frac": hbm_roofline(traffic, ms / 1e3)["frac"]},

@@ -173,6 +173,7 @@ PROTOTYPES = {
                                               vp]),
     "idash_model_intpoly": (status_t, [vp, C.POINTER(vp), C.POINTER(IntpolyParams), C.c_uint64, u64p, u32p, i32p,
                                        C.c_uint64, vp, C.c_int]),
+    "idash_model_intpoly_set_weights": (status_t, [vp, vp, vp]),
     "idash_score_intpoly_device": (status_t, [vp, vp, C.POINTER(RowLayout), C.c_uint64, C.c_uint64, vp,
                                               C.POINTER(RowLayout), vp]),
     "idash_synth_int16_device": (status_t, [vp, C.c_uint64, C.c_uint64, C.c_int32, vp, vp]),

@@ -608,7 +608,7 @@ void make_twiddles(uint32_t N, std::vector<uint32_t> *fwd, std::vector<uint32_t>
 
 struct IntpolyModel {
     uint32_t N = 0, num_samples = 0, region_size = 0;
-    int32_t one = 0;
+    int32_t one = 0, max_abs = 0;
     uint64_t n_out = 0, n_terms = 0, n_rows = 0;
     NttConsts k{};
     uint64_t *d_term_ptr = nullptr;
@@ -681,6 +681,7 @@ extern "C" idash_status idash_model_intpoly(idash_ctx *ctx, idash_model **model,
     ip.num_samples = p->num_samples;
     ip.region_size = p->region_size;
     ip.one = p->one_t32;
+    ip.max_abs = p->max_abs_coef;
     ip.n_out = n_out;
     ip.n_terms = nnz;
     ip.n_rows = n_in_rows;
@@ -750,6 +751,20 @@ extern "C" idash_status idash_model_intpoly(idash_ctx *ctx, idash_model **model,
     ctx->models.insert(m);
     *model = m;
     return IDASH_OK;
+}
+
+extern "C" idash_status idash_model_intpoly_set_weights(idash_model *m, const int16_t *d_term_poly, void *stream) {
+    if (!m) return IDASH_ERR_INVALID_ARGUMENT;
+    idash_ctx *ctx = m->ctx;
+    if (m->form != Form::kIntPoly || !m->intpoly) return ctx->fail(IDASH_ERR_STATE, "not an integer-polynomial model");
+    IntpolyModel &ip = *m->intpoly;
+    if (ip.n_terms == 0) return IDASH_OK;
+    if (!d_term_poly) return IDASH_ERR_INVALID_ARGUMENT;
+    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+    const uint32_t grid = uint32_t(std::min<uint64_t>(ip.n_terms, uint64_t(ctx->sm_count) * 8));
+    k_ntt_model<<<grid, kNttThreads, size_t(4) * ip.N * 4, st>>>(d_term_poly, ip.n_terms, ip.N, ip.d_tw, ip.k,
+                                                                ip.max_abs, ip.d_w_hat, ctx->d_err);
+    return ctx->check_cuda(cudaGetLastError(), "k_ntt_model launch");
 }
 
 extern "C" idash_status idash_score_intpoly_device(idash_model *m, const void *d_in, const idash_row_layout *il,

@@ -385,6 +385,12 @@ class IntpolyModel:
         except Exception:
             pass
 
+    def set_weights(self, d_term_poly: int, stream=None):
+        """New int16 weight polynomials (device memory, [terms][N]) for the
+        same terms, transformed into the resident form asynchronously."""
+        self.ctx.check(self.ctx.lib.idash_model_intpoly_set_weights(self.h, C.c_void_p(d_term_poly),
+                                                                    C.c_void_p(stream) if stream else None))
+
     def score_device(self, d_in: int, in_layout: RowLayout, out_begin: int, out_end: int, d_out: int,
                      out_layout: RowLayout, stream=None):
         self.ctx.check(self.ctx.lib.idash_score_intpoly_device(

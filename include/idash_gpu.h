@@ -313,6 +313,13 @@ idash_status idash_model_intpoly(idash_ctx *ctx, idash_model **model, const idas
                                  uint64_t n_out, const uint64_t *term_ptr, const uint32_t *term_feat,
                                  const int32_t *bias, uint64_t n_in_rows, const int16_t *term_poly,
                                  int term_poly_on_device);
+/* Replaces the model's weights in place: d_term_poly holds new [nnz][N]
+ * int16 polynomials (device memory) for the same terms; they are
+ * transformed into the resident form on `stream` (NULL: the context's),
+ * asynchronously.  A coefficient beyond max_abs_coef is reported by the next
+ * synchronising call as IDASH_ERR_INDEX; that term's resident weights are
+ * then undefined until replaced again. */
+idash_status idash_model_intpoly_set_weights(idash_model *model, const int16_t *d_term_poly, void *stream);
 /* Scores outputs [out_begin, out_end) (output o -> row o - out_begin) from
  * the n_in_rows input TRLWE rows at d_in.  Asynchronous on `stream`. */
 idash_status idash_score_intpoly_device(idash_model *model, const void *d_in, const idash_row_layout *in_layout,

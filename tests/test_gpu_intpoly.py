@@ -120,3 +120,28 @@ def test_exactness_bounds_are_enforced(ctx):
     with pytest.raises(gpu.IdashError):
         gpu.IntpolyModel(ctx, csr, big, 10, 1000, 1024)
     ctx.sync()
+
+
+def test_set_weights_replaces_the_resident_transform(ctx, oracle):
+    """New weights for the same terms, transformed on the device in place:
+    the next product equals the schoolbook product with the new weights, and
+    setting the first weights back restores the first result."""
+    csr, poly, rows, bias = _case(5, 6, 20, 12)
+    m = gpu.IntpolyModel(ctx, csr, poly, 20, 1000, 1024, bias=bias)
+    poly2 = np.random.default_rng(6).integers(-8192, 8192, size=poly.shape).astype(np.int16)
+    d_in = ctx.device_alloc(rows.nbytes)
+    d_in.upload(rows)
+    d_out = ctx.device_alloc(6 * 8192)
+    d_poly = ctx.device_alloc(poly.nbytes)
+    try:
+        for weights in (poly2, poly):
+            d_poly.upload(weights)
+            m.set_weights(d_poly.ptr)
+            m.score_device(d_in.ptr, gpu.DENSE_TRLWE, 0, 6, d_out.ptr, gpu.DENSE_TRLWE)
+            ctx.sync()
+            want = oracle.intpoly_score(csr.term_ptr, csr.term_feat, weights, bias, rows, 1000, 1024, 0, 6)
+            np.testing.assert_array_equal(d_out.download(dtype=np.int32).reshape(6, 2048), want)
+    finally:
+        for b in (d_in, d_out, d_poly):
+            b.free()
+        m.free()
