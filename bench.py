@@ -897,7 +897,8 @@ def run_sections(ctx, args, sections):
     if "intpoly" in sections:
         forms["intpoly"] = section_intpoly(ctx, args.seed + 3, scale=64 if args.small else 1)
     if "serving" in sections:
-        forms["serving"] = section_serving(ctx, args.seed + 2)
+        forms["serving"] = section_serving(ctx, args.seed + 2, **(
+            dict(n_requests=300, e2e_requests=20, lwe_requests=2, cpu_requests=2) if args.small else {}))
     if "files" in sections:
         forms["files"] = section_files(args.seed + 4, small=args.small)
     return forms
@@ -1074,7 +1075,8 @@ def main():
                          "cloud step through its files, is opt-in)")
     ap.add_argument("--no-headline", action="store_true",
                     help="measure only --sections (no headline, e2e or CPU baseline)")
-    ap.add_argument("--small", action="store_true", help="LWE sections at a reduced size (profiling)")
+    ap.add_argument("--small", action="store_true",
+                    help="LWE and int-poly sections at a reduced size, serving with fewer requests (profiling)")
     ap.add_argument("--kernel", type=int, default=None,
                     help="the headline model's kernel option (idash_set_option 'kernel'; default: autotuned)")
     args = ap.parse_args()
