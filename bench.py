@@ -46,6 +46,9 @@ WORKLOADS = {
     "trlwe_prof": dict(n_indiv=1000, n_tags=8000, n_targets=40000, neighbours=5,
                        desc="profiling size, TRLWE-packed: 1,000 individuals, 8,000 tags, 40,000 targets x 3 outputs, "
                             "5 neighbours, NUM_REGIONS=1 (inputs 197 MB > L2)"),
+    "trlwe_n10": dict(n_indiv=1000, n_tags=16184, n_targets=80882, neighbours=10,
+                      desc="full scale, TRLWE-packed, 10 neighbours (the served model): 1,000 individuals, "
+                           "16,184 tags, 80,882 targets x 3 outputs, N=1024, NUM_REGIONS=1"),
     "trlwe_r10": dict(n_indiv=100, n_tags=500, n_targets=2000, neighbours=5,
                       desc="CPU-runnable size, TRLWE-packed: 100 individuals (NUM_REGIONS=10, REGION_SIZE=102), "
                            "500 tags, 2,000 targets x 3 outputs, 5 neighbours"),

@@ -22,8 +22,8 @@ cudaError_t synth_trlwe_rows(uint64_t seed, const idash_trlwe_params &p, uint64_
 // (as idash_synth_uniform_device), row row_begin at d_out.
 cudaError_t fill_uniform_rows(uint64_t seed, uint64_t row_begin, uint64_t n_rows, uint32_t row_words, uint8_t *d_out,
                               uint64_t row_stride, int sm_count, cudaStream_t s);
-// Adds to *d_digest the order-independent digest of n_words output words
-// (sum mod 2^64 of word_hash(index_base + i, word i)).
+// Adds to *d_digest the order-independent digest of n_words output words at
+// global word indices index_base + i (the quad hashes of common.cuh).
 cudaError_t digest_words(const uint32_t *words, uint64_t n_words, uint64_t index_base, uint64_t *d_digest,
                          int sm_count, cudaStream_t s);
 uint64_t digest_host(const uint32_t *words, uint64_t n_words, uint64_t index_base);

@@ -19,13 +19,16 @@ __host__ __device__ __forceinline__ uint64_t mix64(uint64_t z) {
     return z ^ (z >> 31);
 }
 
-// Hash of one output word keyed by its index: for each index a bijection of
-// the word (an added key, then xor-shifts around an odd multiply), all in
-// 32-bit arithmetic.  The serving digest is the sum mod 2^64 of word_hash over
-// a request's output words.  The key of index i + d, when the low word of i
-// does not wrap on adding d, is hash_index_key(i) + d * kHashLo: keys along a
-// row follow by addition.
-constexpr uint32_t kHashLo = 0x85EBCA77u, kHashHi = 0xC2B2AE3Du;
+// The serving digest, in 32-bit arithmetic.  Output words are taken by
+// aligned quads of the output layout (word indices 4Q .. 4Q+3).  A quad's
+// hash starts at its key hash_index_key(Q), takes h = h * kHashMul + w for
+// each of its words present, in index order, and ends with hash_finish (xor-
+// shifts around an odd multiply).  The digest is the sum mod 2^64 of the
+// quads' hashes: order-independent across launches, and changed by any word,
+// by moving a word within its quad or to another quad.  The key of quad Q + d,
+// when the low word of Q does not wrap on adding d, is hash_index_key(Q) +
+// d * kHashLo: keys along a row follow by addition.
+constexpr uint32_t kHashLo = 0x85EBCA77u, kHashHi = 0xC2B2AE3Du, kHashMul = 0x9E3779B1u;
 
 __host__ __device__ __forceinline__ uint32_t hash_index_key(uint64_t index) {
     return uint32_t(index) * kHashLo + uint32_t(index >> 32) * kHashHi;
@@ -38,9 +41,7 @@ __host__ __device__ __forceinline__ uint32_t hash_finish(uint32_t x) {
     return x;
 }
 
-__host__ __device__ __forceinline__ uint32_t word_hash(uint64_t index, uint32_t w) {
-    return hash_finish(w + hash_index_key(index));
-}
+__host__ __device__ __forceinline__ uint32_t hash_step(uint32_t h, uint32_t w) { return h * kHashMul + w; }
 
 // ~1 s at the GB300's 2.07 GHz maximum SM clock.
 constexpr long long kWaitLimitCycles = 2000000000ll;

@@ -161,31 +161,46 @@ __device__ __forceinline__ void write_outputs(const ScoreArgs &a, const PlanGrou
     }
 }
 
-// The fused digest: adds word_hash(index, word) of every word write_outputs
-// stored (acc holds the stored values) to `dig`.  When the low word of the
-// slice's first index leaves room for W more, every key of the slice is that
-// index's key plus (column offset) * kHashLo.
+// The fused digest: adds the quad hashes (common.cuh) of the words
+// write_outputs stored (acc holds the stored values) to `dig`.  A thread's
+// quad k starts at word c0 + 4*lane + 4*k*TEAM of its row, a multiple of 4 of
+// the output layout (digest_base, the row stride and c0 are), so each quad is
+// hashed whole from registers.  When the low word of the slice's first quad
+// index leaves room for the slice, every key is that index's key plus a
+// constant.
 template <int W, int G, int Q, int TEAM>
 __device__ __forceinline__ void digest_outputs(const ScoreArgs &a, const PlanGroup &gr,
                                                const uint32_t (&acc)[G][4 * Q], uint32_t c0, uint32_t lane,
                                                uint32_t valid, uint64_t &dig) {
     const uint64_t row_words = a.out_stride / 4;
+    const uint32_t lo = uint32_t(min(a.out_lo, uint64_t(kNoOutput)));
+    const uint32_t hi = uint32_t(min(a.out_hi, uint64_t(kNoOutput)));
 #pragma unroll
     for (int m = 0; m < G; ++m) {
         const uint32_t o = gr.out[m];
-        if (o == kNoOutput || o < a.out_lo || o >= a.out_hi) continue;
-        const uint64_t r = a.out_row_map ? uint64_t(a.out_row_map[o]) : uint64_t(o) - a.out_row_base;
-        const uint64_t base = a.digest_base + r * row_words + c0;
-        const bool flat = uint32_t(base) <= 0xFFFFFFFFu - uint32_t(W);
-        const uint32_t key_lane = hash_index_key(base) + 4 * lane * kHashLo;
+        if (o - lo >= hi - lo) continue;  // outside [out_lo, out_hi), kNoOutput included
+        const uint32_t r = a.out_row_map ? a.out_row_map[o] : o - uint32_t(a.out_row_base);
+        const uint64_t quad0 = (a.digest_base + uint64_t(r) * row_words + c0) / 4;  // the slice's first quad
+        if (valid >= W && uint32_t(quad0) <= 0xFFFFFFFFu - uint32_t(W / 4)) {
+            const uint32_t key0 = hash_index_key(quad0) + lane * kHashLo;
 #pragma unroll
-        for (int k = 0; k < Q; ++k) {
-            const uint32_t q = 4 * lane + 4 * k * TEAM;
-            const uint32_t key = flat ? key_lane + uint32_t(4 * k * TEAM) * kHashLo : hash_index_key(base + q);
+            for (int k = 0; k < Q; ++k) {
+                uint32_t h = key0 + uint32_t(k * TEAM) * kHashLo;
 #pragma unroll
-            for (int e = 0; e < 4; ++e)
-                if (q + 4 <= valid || q + e < valid)
-                    dig += hash_finish(acc[m][4 * k + e] + key + uint32_t(e) * kHashLo);
+                for (int e = 0; e < 4; ++e) h = hash_step(h, acc[m][4 * k + e]);
+                dig += hash_finish(h);
+            }
+        } else {
+#pragma unroll
+            for (int k = 0; k < Q; ++k) {
+                const uint32_t q = 4 * lane + 4 * k * TEAM;
+                if (q >= valid) continue;
+                uint32_t h = hash_index_key(quad0 + q / 4);
+#pragma unroll
+                for (int e = 0; e < 4; ++e)
+                    if (q + e < valid) h = hash_step(h, acc[m][4 * k + e]);
+                dig += hash_finish(h);
+            }
         }
     }
 }
@@ -607,6 +622,7 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_score_ws(const ScoreArgs a) {
         uint32_t pending = 0;  // stages with copies not yet consumed
         uint32_t it = 0;
         uint32_t tile = 0;
+        uint32_t job = 0;  // multi-job launches: the job of the last tile
         if (lane == 0) tile = atomicAdd(a.tile_counter, 1u);
         tile = __shfl_sync(0xFFFFFFFFu, tile, 0);
         for (;; ++it) {
@@ -626,9 +642,12 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_score_ws(const ScoreArgs a) {
                 return;
             }
             ScoreArgs aj = a;
-            uint32_t lt = tile, job = 0;
+            uint32_t lt = tile;
             if (DIG && a.n_jobs) {
-                job = job_of(a, tile);
+                // a CTA's tiles come from one counter in increasing order, so
+                // its job index only moves forward
+                if (a.jobs[job].tile_begin > tile) job = job_of(a, tile);
+                while (job + 1 < a.n_jobs && a.jobs[job + 1].tile_begin <= tile) ++job;
                 with_job(aj, a.jobs[job], lt);
             }
             const PlanBlock blk = aj.blocks[aj.block_lo + lt % aj.n_blocks];

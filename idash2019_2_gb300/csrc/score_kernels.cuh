@@ -56,9 +56,9 @@ struct ScoreArgs {
     uint32_t accumulate;          // 1: add to the outputs (later parts of split groups)
     uint32_t *tile_counter;       // persistent kernel: next tile (zeroed before launch)
     uint32_t *err;                // device error word
-    // k_score_ws with the fused digest only (null otherwise): the sum mod 2^64
-    // of word_hash(digest_base + r * out_stride / 4 + c, word) over the words
-    // written, row r and column c, is added to *digest.
+    // k_score_ws with the fused digest only (null otherwise): the digest of
+    // the words written (the quad hashes of common.cuh), word (r, c) at
+    // global index digest_base + r * out_stride / 4 + c, is added to *digest.
     unsigned long long *digest;
     uint64_t digest_base;         // a multiple of 4
     // KernelKind::kTc only.  tc_a: per block, the coefficient digits in the

@@ -117,25 +117,29 @@ __global__ void k_synth_trlwe(uint64_t seed, uint32_t N, uint32_t num_samples, u
     }
 }
 
-// Order-independent digest of a request's output words: the sum mod 2^64 of
-// word_hash(global index, word) over every word, accumulated into *digest.
+// Order-independent digest of a request's output words (the quad hashes of
+// common.cuh, global word indices index_base + i), accumulated into *digest.
 // A pass over the outputs, for scoring kernels that do not take the digest
-// as they store (the warp-specialised one does).  16-byte loads and 32-bit
-// arithmetic stream it at close to the HBM copy rate.
+// as they store (the warp-specialised one does).  One thread per quad; a
+// whole quad at a 16-byte aligned address is one 16-byte load.
 __global__ void k_digest(const uint32_t *words, uint64_t n_words, uint64_t index_base,
                          unsigned long long *digest) {
     uint64_t acc = 0;
     const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
     const uint64_t first = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    // quads when the words start 16-byte aligned, then the tail one by one
-    const uint64_t n4 = (reinterpret_cast<uintptr_t>(words) & 15u) == 0 ? n_words / 4 : 0;
-    const uint4 *w4 = reinterpret_cast<const uint4 *>(words);
-    for (uint64_t q = first; q < n4; q += stride) {
-        const uint4 v = w4[q];
-        const uint64_t i = index_base + 4 * q;
-        acc += uint64_t(word_hash(i, v.x)) + word_hash(i + 1, v.y) + word_hash(i + 2, v.z) + word_hash(i + 3, v.w);
+    const uint64_t end = index_base + n_words, q0 = index_base >> 2, q_end = (end + 3) >> 2;
+    for (uint64_t q = q0 + first; q < q_end; q += stride) {
+        const uint64_t lo = q * 4 > index_base ? q * 4 : index_base, hi = q * 4 + 4 < end ? q * 4 + 4 : end;
+        const uint32_t *w = words + (lo - index_base);
+        uint32_t h = hash_index_key(q);
+        if (hi - lo == 4 && (reinterpret_cast<uintptr_t>(w) & 15u) == 0) {
+            const uint4 v = *reinterpret_cast<const uint4 *>(w);
+            h = hash_step(hash_step(hash_step(hash_step(h, v.x), v.y), v.z), v.w);
+        } else {
+            for (uint64_t i = lo; i < hi; ++i) h = hash_step(h, w[i - lo]);
+        }
+        acc += hash_finish(h);
     }
-    for (uint64_t i = 4 * n4 + first; i < n_words; i += stride) acc += word_hash(index_base + i, words[i]);
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xFFFFFFFFu, acc, off);
     if ((threadIdx.x & 31) == 0) atomicAdd(digest, (unsigned long long)acc);
@@ -195,7 +199,14 @@ cudaError_t digest_words(const uint32_t *words, uint64_t n_words, uint64_t index
 
 uint64_t digest_host(const uint32_t *words, uint64_t n_words, uint64_t index_base) {
     uint64_t acc = 0;
-    for (uint64_t i = 0; i < n_words; ++i) acc += word_hash(index_base + i, words[i]);
+    for (uint64_t i = 0; i < n_words;) {
+        uint32_t h = hash_index_key((index_base + i) >> 2);
+        do {
+            h = hash_step(h, words[i]);
+            ++i;
+        } while (i < n_words && ((index_base + i) & 3u) != 0);
+        acc += hash_finish(h);
+    }
     return acc;
 }
 

@@ -220,9 +220,9 @@ typedef struct {
     double admit_s;        /* admission, seconds after idash_server_open (host clock) */
     double done_s;         /* completion: outputs in h_out (or scored), seconds after open (CUDA events) */
     uint64_t device_bytes; /* HBM the request held at admission (inputs + one output segment) */
-    uint64_t digest;       /* sum mod 2^64 over its output words of a 32-bit hash of (index, word),
-                              index = word position in the output layout above; idash_digest_host
-                              restates it */
+    uint64_t digest;       /* sum mod 2^64, over the aligned quads of its output words (word
+                              positions 4Q .. 4Q+3 in the output layout above), of a 32-bit hash
+                              of (Q, the quad's words); idash_digest_host restates it */
 } idash_request_result;
 
 idash_status idash_server_open(idash_model *model, const idash_serve_config *config, idash_server **server);

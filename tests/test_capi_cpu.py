@@ -79,32 +79,51 @@ def test_synth_model_rejects_bad_spec(lib):
     assert lib.idash_synth_model(C.byref(spec), C.byref(m)) == 1
 
 
-def _word_hash(index, w):
-    """The serving digest's word hash restated in numpy (32-bit lanes): key =
-    lo(index) * 0x85EBCA77 + hi(index) * 0xC2B2AE3D, x = w + key, then
-    x ^= x >> 15, x *= 0x2C1B3C6D, x ^= x >> 12."""
-    index = np.asarray(index, np.uint64)
-    lo = (index & np.uint64(0xFFFFFFFF)).astype(np.uint32)
-    hi = (index >> np.uint64(32)).astype(np.uint32)
-    x = np.asarray(w, np.uint32) + lo * np.uint32(0x85EBCA77) + hi * np.uint32(0xC2B2AE3D)
-    x ^= x >> np.uint32(15)
-    x *= np.uint32(0x2C1B3C6D)
-    x ^= x >> np.uint32(12)
-    return x
+def _digest(words, index_base):
+    """The serving digest restated in numpy (32-bit lanes): words at global
+    indices index_base + i, taken by aligned quads Q = index // 4; a quad's
+    hash starts at lo(Q) * 0x85EBCA77 + hi(Q) * 0xC2B2AE3D, takes
+    h = h * 0x9E3779B1 + w for each of its words present in index order, and
+    ends with h ^= h >> 15, h *= 0x2C1B3C6D, h ^= h >> 12; the digest is the
+    sum of the quad hashes mod 2^64."""
+    idx = np.uint64(index_base) + np.arange(words.size, dtype=np.uint64)
+    quad = idx >> np.uint64(2)
+    qs, first = np.unique(quad, return_index=True)
+    lo = (qs & np.uint64(0xFFFFFFFF)).astype(np.uint32)
+    hi = (qs >> np.uint64(32)).astype(np.uint32)
+    h = lo * np.uint32(0x85EBCA77) + hi * np.uint32(0xC2B2AE3D)
+    ends = np.append(first[1:], words.size)
+    for step in range(4):  # the quad's words in index order
+        pos = first + step
+        live = pos < ends
+        h[live] = h[live] * np.uint32(0x9E3779B1) + words[pos[live]]
+    h ^= h >> np.uint32(15)
+    h *= np.uint32(0x2C1B3C6D)
+    h ^= h >> np.uint32(12)
+    return int(h.astype(np.uint64).sum(dtype=np.uint64))
 
 
-@pytest.mark.parametrize("index_base", [0, 1 << 20, (1 << 32) - 5, 3 << 33])
-def test_digest_host_restates_the_word_hash(lib, index_base):
+@pytest.mark.parametrize("index_base,n", [(0, 1000), (1 << 20, 1000), ((1 << 34) - 6, 1000), (3 << 33, 999),
+                                          (7, 13), (5, 2), (0, 1)])
+def test_digest_host_restates_the_quad_hash(lib, index_base, n):
     """idash_digest_host (the host restatement the serving tests check the
-    device digests against) is the sum mod 2^64 of the word hash, including
-    where the index crosses 2^32."""
+    device digests against) is the sum mod 2^64 of the quad hashes, with
+    partial quads at either end and where the quad index crosses 2^32; and
+    the digest of a buffer is the sum of the digests of its pieces when they
+    are cut at quad boundaries."""
     import ctypes as C
-    words = np.random.default_rng(index_base % 1000).integers(0, 2 ** 32, 1000, dtype=np.uint64).astype(np.uint32)
+    words = np.random.default_rng(index_base % 1000 + n).integers(0, 2 ** 32, n, dtype=np.uint64).astype(np.uint32)
     with np.errstate(over="ignore"):
-        h = _word_hash(np.uint64(index_base) + np.arange(words.size, dtype=np.uint64), words)
-    want = int(h.astype(np.uint64).sum(dtype=np.uint64))
-    got = lib.idash_digest_host(words.ctypes.data_as(C.POINTER(C.c_uint32)), words.size, index_base)
+        want = _digest(words, index_base)
+    P = C.POINTER(C.c_uint32)
+    got = lib.idash_digest_host(words.ctypes.data_as(P), words.size, index_base)
     assert got == want
+    cut = (4 - index_base % 4) % 4 + 4 * (n // 8)
+    if 0 < cut < n:
+        a, b = np.ascontiguousarray(words[:cut]), np.ascontiguousarray(words[cut:])
+        parts = lib.idash_digest_host(a.ctypes.data_as(P), a.size, index_base) + \
+            lib.idash_digest_host(b.ctypes.data_as(P), b.size, index_base + cut)
+        assert parts % (1 << 64) == got
 
 
 @pytest.mark.parametrize("spec", [dict(n_tags=200, n_targets=500, neighbours=5),
