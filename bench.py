@@ -892,6 +892,12 @@ def run_sections(ctx, args, sections):
     forms = {}
     if "config1" in sections:
         forms["config1"] = section_config1(ctx, args.seed + 5)
+    # serving before the LWE and integer-polynomial forms: its host-payload
+    # leg pins about 20 GB of host memory, and after those forms' 100+ GB
+    # device working sets its copies measured at half the host link's rate
+    if "serving" in sections:
+        forms["serving"] = section_serving(ctx, args.seed + 2, **(
+            dict(n_requests=300, e2e_requests=20, lwe_requests=2, cpu_requests=2) if args.small else {}))
     if "lwe_full" in sections:
         forms["lwe_full"] = section_lwe(ctx, args.seed, ni, nt, ng, neighbours=5, cpu_outputs=512)
     if "batched_uneven" in sections:
@@ -899,9 +905,6 @@ def run_sections(ctx, args, sections):
                                               cpu_outputs=192)
     if "intpoly" in sections:
         forms["intpoly"] = section_intpoly(ctx, args.seed + 3, scale=64 if args.small else 1)
-    if "serving" in sections:
-        forms["serving"] = section_serving(ctx, args.seed + 2, **(
-            dict(n_requests=300, e2e_requests=20, lwe_requests=2, cpu_requests=2) if args.small else {}))
     if "files" in sections:
         forms["files"] = section_files(args.seed + 4, small=args.small)
     return forms
