@@ -545,6 +545,7 @@ const char *idash_status_string(idash_status s) {
         case IDASH_ERR_UNSUPPORTED: return "unsupported parameters";
         case IDASH_ERR_ADMISSION: return "request exceeds the HBM budget";
         case IDASH_ERR_STATE: return "invalid call order";
+        case IDASH_PENDING: return "request still in flight";
     }
     return "unknown status";
 }

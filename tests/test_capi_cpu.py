@@ -25,8 +25,10 @@ def test_library_exports_every_declared_function(lib):
 
 
 def test_status_strings(lib):
-    for code in range(11):
-        assert lib.idash_status_string(code)
+    """Every status the header declares has its own string."""
+    strings = [lib.idash_status_string(code) for code in range(len(_lib.STATUS))]
+    assert all(strings) and b"unknown status" not in strings
+    assert len(set(strings)) == len(strings)
 
 
 def test_open_without_device_is_a_status(lib):
