@@ -260,3 +260,56 @@ def test_online_server_refuses_bad_requests(served):
         assert srv.poll(t)["digest"] == r["digest"]
     finally:
         srv.close()
+
+
+def test_submits_from_several_threads_and_close_drains(served):
+    """Four client threads submit and wait at once (the calls release the
+    interpreter lock): every request's outputs and digest are right.  Then
+    requests submitted and not waited for are finished by close."""
+    import ctypes as C
+    import threading
+    ctx, w, m, _, _, _ = served
+    srv = gpu.Server(m, hbm_budget=1 << 30, max_inflight=6)
+    results, errors = {}, []
+
+    def client(k):
+        try:
+            rng = np.random.default_rng(100 + k)
+            for i in range(4):
+                length = int(rng.integers(10, 200))
+                t0 = int(rng.integers(0, 1000 - length))
+                n_indiv = int(rng.integers(1, 1500))
+                in_shape, out_shape, lo = gpu.serve_input_shape(m, n_indiv, t0, t0 + length)
+                h_in = _rows_for(rng, in_shape)
+                h_out = np.zeros(out_shape, np.int32)
+                r = srv.wait(srv.submit(n_indiv, t0, t0 + length, h_in=h_in, h_out=h_out))
+                results[(k, i)] = (n_indiv, t0, t0 + length, h_in, h_out, lo, r)
+        except Exception as e:  # reported by the main thread
+            errors.append(e)
+
+    threads = [threading.Thread(target=client, args=(k,)) for k in range(4)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    assert not errors and len(results) == 16
+    for n_indiv, t0, t1, h_in, h_out, lo, r in results.values():
+        words = np.ascontiguousarray(h_out).view(np.uint32).ravel()
+        assert r["digest"] == ctx.lib.idash_digest_host(words.ctypes.data_as(C.POINTER(C.c_uint32)), words.size, 0)
+    # one request per thread against the oracle
+    for k in range(4):
+        n_indiv, t0, t1, h_in, h_out, lo, _ = results[(k, 0)]
+        sub = w.model.slice_outputs(3 * t0, 3 * t1)
+        rows = np.zeros((900, 2048), np.int32)
+        rows[lo:lo + h_in.shape[1]] = h_in[0]
+        want, _ = oracle_trlwe(sub, rows, min(1024, n_indiv))
+        np.testing.assert_array_equal(h_out[0], want)
+    for i in range(8):
+        srv.submit(50 + i, 10 * i, 10 * i + 300, seed=i + 1)
+    srv.close()  # returns once the eight are scored
+    assert srv.h is None
+
+
+def oracle_trlwe(sub, rows, ns):
+    import pyoracle
+    return pyoracle.trlwe_score(sub.term_ptr, sub.term_feat, sub.term_coef, rows, ns, 1, 1024)
